@@ -1,0 +1,869 @@
+/*
+ * scft_ctx.cu — the C ABI of include/scft_gpu.h: context set-up, device
+ * memory, the per-iteration launch sequence and host transfers.
+ *
+ * One iteration (SCFT.c:1090-1580) is launched as
+ *   iter_begin (iIter++, Boltzmann factors, initial slices)
+ *   for s in 0 .. maxlen-2: one pass per grid axis over every active chain
+ *   iter_end   (Q, densities, fused update, finalize, p shift)
+ * on the context's own stream; with use_graph the sequence is captured once
+ * and replayed. Every instance of a context shares grid and contour counts.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "scft_internal.h"
+
+static thread_local char g_err[512] = "";
+
+static void set_err(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char *scft_last_error(void) { return g_err; }
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+            return e_ == cudaErrorMemoryAllocation ? SCFT_ERR_OOM : SCFT_ERR_CUDA;                 \
+        }                                                                                          \
+    } while (0)
+
+struct Axis {
+    AxisGeom g;
+    int tile;
+    int ntiles;
+    int h, even;
+    void *spec, *tw, *kA, *kB; /* device arrays in the context's precision */
+};
+
+struct scft_ctx {
+    scft_options opt;
+    int B = 0;
+    int psize = 8;
+    int sms = 152;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<scft_surface> surf;
+    std::vector<scft_derived> der;
+    long m = 0, sm = 0;
+    int nx = 0, ny = 0, nz = 0;
+    int nchains = 0, nblocks = 0, maxlen = 0;
+    unsigned field_use = 0;
+    std::vector<ChainDesc> chains_h; /* [B * nchains] */
+    std::vector<BlockDesc> blocks_h;
+    SpeciesDesc species_h[SCFT_NSPECIES];
+    std::vector<Axis> axes;
+    /* device memory */
+    double *w = nullptr, *phi = nullptr, *raw = nullptr, *mask = nullptr, *partial = nullptr, *noise = nullptr;
+    void *bz = nullptr;
+    InstParams *params = nullptr;
+    InstState *state = nullptr;
+    ChainDesc *chains = nullptr;
+    BlockDesc *blocks = nullptr;
+    SpeciesDesc *species = nullptr;
+    scft_iter_out *hist = nullptr;
+    scft_iter_out *hist_host = nullptr; /* pinned */
+    int hist_cap = 0;
+    int nparts = 0;
+    size_t device_bytes = 0;
+    std::vector<void *> allocs;
+    /* host mirrors */
+    std::vector<unsigned long> iter;
+    std::vector<unsigned short> rng; /* 3 per instance */
+    std::vector<int> fields_set;
+    /* graph */
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    /* timing */
+    int timing = 0;
+    std::vector<cudaEvent_t> ev; /* 2 per iteration slot + 2 overall */
+    scft_timing last_timing{};
+    long launches_per_iter = 0, prop_launches_per_iter = 0;
+};
+
+static int dalloc(scft_ctx *c, void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        set_err("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        *p = nullptr;
+        return SCFT_ERR_OOM;
+    }
+    c->allocs.push_back(*p);
+    c->device_bytes += bytes;
+    cudaMemsetAsync(*p, 0, bytes, c->stream);
+    return SCFT_OK;
+}
+
+extern "C" void scft_options_default(scft_options *o)
+{
+    memset(o, 0, sizeof(*o));
+    o->precision = SCFT_PREC_FP64;
+    o->device = 0;
+    o->noise_mode = SCFT_NOISE_HOST;
+    o->use_graph = 0;
+    o->n_instances = 1;
+}
+
+/* ------------------------------------------------------- shape helpers */
+static const int DBK_FX[4] = {0, 3, 5, 7};
+
+/* Radix decomposition for the Stockham FFT: 4s, then 2, then 3s. Returns 0
+ * if n has another prime factor (the axis then uses the dense operator). */
+static int radices(int n, int *rad, int *nrad)
+{
+    int k = 0;
+    while (n % 4 == 0 && k < SCFT_MAX_RADIX_STAGES) {
+        rad[k++] = 4;
+        n /= 4;
+    }
+    while (n % 2 == 0 && k < SCFT_MAX_RADIX_STAGES) {
+        rad[k++] = 2;
+        n /= 2;
+    }
+    while (n % 3 == 0 && k < SCFT_MAX_RADIX_STAGES) {
+        rad[k++] = 3;
+        n /= 3;
+    }
+    *nrad = k;
+    return n == 1;
+}
+
+/* k of spectral index t on a periodic axis of length n, as the reference
+ * computes it for aExpArg: 2 pi (n/2 - |t - n/2|) / n (SCFT.c:993-995). */
+static double kval(int t, int n) { return 2.0 * M_PI * (n / 2.0 - fabs(t - n / 2.0)) / n; }
+
+/* Dense 1-D operator of one axis, n x n, row-major K[i*n + j]. */
+static void dense_operator(int n, double alpha, int dirichlet, std::vector<long double> &K)
+{
+    K.assign((size_t)n * n, 0.0L);
+    if (dirichlet) {
+        /* odd extension of length N = 2(n+1): K = (2/L) sum_m E_m sin(pi m a/L) sin(pi m b/L) */
+        const int L = n + 1, N = 2 * L;
+        std::vector<long double> E(n + 1);
+        for (int m = 1; m <= n; ++m) {
+            const double kz = kval(m, N);
+            E[m] = expl(-(long double)alpha * (long double)kz * (long double)kz);
+        }
+        const long double pi = 3.141592653589793238462643383279502884L;
+        for (int a = 0; a < n; ++a)
+            for (int b = a; b < n; ++b) {
+                long double s = 0.0L;
+                for (int m = 1; m <= n; ++m)
+                    s += E[m] * sinl(pi * m * (a + 1) / L) * sinl(pi * m * (b + 1) / L);
+                s *= 2.0L / L;
+                K[(size_t)a * n + b] = s;
+                K[(size_t)b * n + a] = s;
+            }
+    } else {
+        /* circulant: K[i][j] = (1/n) sum_t E_t cos(2 pi t (i-j) / n) */
+        const long double pi = 3.141592653589793238462643383279502884L;
+        std::vector<long double> c(n);
+        for (int d = 0; d < n; ++d) {
+            long double s = 0.0L;
+            for (int t = 0; t < n; ++t) {
+                const double k = kval(t, n);
+                s += expl(-(long double)alpha * k * k) * cosl(2.0L * pi * t * d / n);
+            }
+            c[d] = s / n;
+        }
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) K[(size_t)i * n + j] = c[(i - j + n) % n];
+    }
+}
+
+template <typename T>
+static int upload(scft_ctx *c, void **dst, const std::vector<T> &v)
+{
+    int rc = dalloc(c, dst, sizeof(T) * v.size());
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c->stream));
+    return SCFT_OK;
+}
+
+/* Convert a double vector to the context precision and upload. */
+static int upload_p(scft_ctx *c, void **dst, const std::vector<double> &v)
+{
+    if (c->psize == 8) return upload(c, dst, v);
+    std::vector<float> f(v.begin(), v.end());
+    return upload(c, dst, f);
+}
+
+static int pick_tile(long lines_per_chain, long inner_or_lines, int total_chains, int sms, int start)
+{
+    int tile = start;
+    while (tile > 2 && (inner_or_lines % tile != 0 || (lines_per_chain / tile) * (long)total_chains < 2L * sms)) tile /= 2;
+    while (tile > 1 && inner_or_lines % tile != 0) tile /= 2;
+    return tile;
+}
+
+static int build_axes(scft_ctx *c)
+{
+    const scft_derived &d = c->der[0];
+    const int dims[3] = {d.nx, d.ny, d.nz};
+    const double alphas[3] = {d.alphax, d.alphay, d.alphaz};
+    const int total_chains = c->B * c->nchains;
+    for (int ax = 0; ax < 3; ++ax) {
+        const int n = dims[ax];
+        if (n <= 1) continue;
+        Axis A;
+        memset(&A, 0, sizeof(A));
+        A.g.n = n;
+        A.g.ls = ax == 0 ? d.ny * d.nz : (ax == 1 ? d.nz : 1);
+        A.g.inner = ax == 2 ? 1 : A.g.ls;
+        A.g.outer = ax == 0 ? 1 : (ax == 1 ? d.nx : d.nx * d.ny);
+        const int dirichlet = (ax == 2 && c->surf[0].mask);
+        int fft_ok = !dirichlet && radices(n, A.g.rad, &A.g.nrad);
+        A.g.dirichlet = fft_ok ? 0 : 1;
+        const long lines = c->m / n;
+        const long divisor = ax == 2 ? lines : A.g.inner;
+        if (fft_ok) {
+            A.tile = pick_tile(lines, divisor, total_chains, c->sms, c->psize == 8 ? 16 : 32);
+            std::vector<double> spec(n), tw(2 * n);
+            for (int t = 0; t < n; ++t) {
+                const double k = kval(t, n);
+                spec[t] = exp(-alphas[ax] * k * k) / n;
+                tw[2 * t] = cos(2.0 * M_PI * t / n);
+                tw[2 * t + 1] = -sin(2.0 * M_PI * t / n);
+            }
+            int rc = upload_p(c, &A.spec, spec);
+            if (!rc) rc = upload_p(c, &A.tw, tw);
+            if (rc) return rc;
+        } else {
+            A.tile = pick_tile(lines, divisor, total_chains, c->sms, c->psize == 8 ? 8 : 16);
+            std::vector<long double> K;
+            dense_operator(n, alphas[ax], dirichlet, K);
+            A.even = (n % 2 == 0);
+            if (A.even) {
+                const int h = n / 2;
+                A.h = h;
+                std::vector<double> At((size_t)h * h), Bt((size_t)h * h);
+                for (int i = 0; i < h; ++i)
+                    for (int j = 0; j < h; ++j) {
+                        const long double kij = K[(size_t)i * n + j], kim = K[(size_t)i * n + (n - 1 - j)];
+                        At[(size_t)j * h + i] = (double)((kij + kim) / 2.0L);
+                        Bt[(size_t)j * h + i] = (double)((kij - kim) / 2.0L);
+                    }
+                int rc = upload_p(c, &A.kA, At);
+                if (!rc) rc = upload_p(c, &A.kB, Bt);
+                if (rc) return rc;
+            } else {
+                A.h = n;
+                std::vector<double> Kt((size_t)n * n);
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) Kt[(size_t)j * n + i] = (double)K[(size_t)i * n + j];
+                int rc = upload_p(c, &A.kA, Kt);
+                if (rc) return rc;
+                A.kB = A.kA;
+            }
+        }
+        const size_t smem = scft_pass_smem_bytes(A.g, A.tile, A.h, c->psize);
+        int optin_limit = 0;
+        cudaDeviceGetAttribute(&optin_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+        if (smem > (size_t)optin_limit) {
+            set_err("axis %d of length %d needs %zu bytes of shared memory", ax, n, smem);
+            return SCFT_ERR_PARAM;
+        }
+        A.ntiles = (int)(lines / A.tile);
+        c->axes.push_back(A);
+    }
+    /* the limit is a cap, not a reservation: set the device maximum once */
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    CK(scft_pass_configure(optin));
+    return SCFT_OK;
+}
+
+/* Check that every instance has the same shape as instance 0. */
+static int same_shape(const scft_surface &a, const scft_derived &da, const scft_surface &b, const scft_derived &db)
+{
+    if (da.nx != db.nx || da.ny != db.ny || da.nz != db.nz || a.mask != b.mask || a.ns != b.ns) return 0;
+    if (memcmp(da.ns_dbk, db.ns_dbk, sizeof(da.ns_dbk)) || memcmp(da.ns_dbk_x, db.ns_dbk_x, sizeof(da.ns_dbk_x)) ||
+        memcmp(da.ns_homo, db.ns_homo, sizeof(da.ns_homo)) || memcmp(da.ns_s, db.ns_s, sizeof(da.ns_s)))
+        return 0;
+    if (da.alphax != db.alphax || da.alphay != db.alphay || da.alphaz != db.alphaz) return 0;
+    if (a.enable_seed != b.enable_seed || da.n_active != db.n_active || memcmp(da.active, db.active, sizeof(da.active)))
+        return 0;
+    return 1;
+}
+
+static void fill_params(const scft_surface &s, const scft_derived &d, const std::vector<BlockDesc> &blocks,
+                        const SpeciesDesc *species, InstParams &ip)
+{
+    memset(&ip, 0, sizeof(ip));
+    memcpy(ip.chi, d.chi_eff, sizeof(ip.chi));
+    memcpy(ip.phi_avg, d.phi_avg, sizeof(ip.phi_avg));
+    const double coat = d.coating_vol;
+    for (size_t k = 0; k < blocks.size(); ++k) {
+        const BlockDesc &bd = blocks[k];
+        double frac;
+        if (bd.species < 4)
+            frac = s.vol_dbk[bd.species] * (1.0 - coat);
+        else if (bd.species < 14)
+            frac = s.vol_homo[bd.species - 4] * (1.0 - coat);
+        else
+            frac = s.vol_s[bd.species - 14];
+        ip.frac[k] = frac > 0.0 ? frac : 1.0; /* funVolFrac scales only for frac > 0 */
+    }
+    for (int sp = 0; sp < SCFT_NSPECIES; ++sp) {
+        if (!species[sp].present) continue;
+        if (sp < 4)
+            ip.lnq_coef[sp] = (s.vol_dbk[sp] / d.alpha_dbk[sp] * (1.0 - coat));
+        else if (sp < 14)
+            ip.lnq_coef[sp] = (s.vol_homo[sp - 4] / d.alpha_homo[sp - 4] * (1.0 - coat));
+        else
+            ip.lnq_coef[sp] = s.vol_s[sp - 14] / d.alpha_s[sp - 14];
+    }
+    ip.g1 = s.g1;
+    ip.g2 = s.g1 / 6.0;
+    ip.dt_noise = s.dt_noise;
+    ip.ds = d.ds;
+    ip.relaxation = s.relaxation;
+    memcpy(ip.active, d.active, sizeof(ip.active));
+    ip.n_active = d.n_active;
+    ip.enable_seed = s.enable_seed;
+    ip.seed_steps = s.seed_steps;
+    ip.seed_area_delta = s.seed_area_delta;
+    ip.mask = s.mask;
+}
+
+extern "C" int scft_ctx_destroy(scft_ctx *c)
+{
+    if (!c) return SCFT_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->hist_host) cudaFreeHost(c->hist_host);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return SCFT_OK;
+}
+
+extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options *opt_in, scft_ctx **out)
+{
+    if (!surfaces || !out) return SCFT_ERR_PARAM;
+    *out = nullptr;
+    scft_options opt;
+    if (opt_in)
+        opt = *opt_in;
+    else
+        scft_options_default(&opt);
+    if (opt.n_instances < 1) opt.n_instances = 1;
+    if (opt.precision != SCFT_PREC_FP64 && opt.precision != SCFT_PREC_FP32) return SCFT_ERR_PARAM;
+    if (opt.noise_mode != SCFT_NOISE_HOST) {
+        set_err("noise_mode %d is not available in this build", opt.noise_mode);
+        return SCFT_ERR_PARAM;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_err("no CUDA device");
+        return SCFT_ERR_NODEV;
+    }
+    if (opt.device < 0 || opt.device >= ndev) return SCFT_ERR_PARAM;
+
+    scft_ctx *c = new scft_ctx();
+    c->opt = opt;
+    c->B = opt.n_instances;
+    c->psize = opt.precision == SCFT_PREC_FP64 ? 8 : 4;
+    c->device = opt.device;
+    cudaSetDevice(opt.device);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, opt.device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_err("cudaStreamCreate failed");
+        delete c;
+        return SCFT_ERR_CUDA;
+    }
+    c->surf.assign(surfaces, surfaces + c->B);
+    c->der.resize(c->B);
+    for (int b = 0; b < c->B; ++b) {
+        int rc = scft_derive(&c->surf[b], &c->der[b]);
+        if (rc != SCFT_OK) {
+            set_err("instance %d: parameter derivation failed (%d)", b, rc);
+            scft_ctx_destroy(c);
+            return rc;
+        }
+        if (b > 0 && !same_shape(c->surf[0], c->der[0], c->surf[b], c->der[b])) {
+            set_err("instance %d differs in grid or contour counts from instance 0", b);
+            scft_ctx_destroy(c);
+            return SCFT_ERR_PARAM;
+        }
+    }
+    const scft_derived &d = c->der[0];
+    const scft_surface &s = c->surf[0];
+    c->nx = d.nx;
+    c->ny = d.ny;
+    c->nz = d.nz;
+    c->m = d.m;
+    c->sm = (d.m + 63) / 64 * 64;
+
+    /* chains, blocks, species (one instance's worth; identical across instances) */
+    struct ChainSpec {
+        int len, f0, f1, seg_end, init, init_arg;
+    };
+    std::vector<ChainSpec> cs;
+    std::vector<BlockDesc> blocks;
+    memset(c->species_h, 0, sizeof(c->species_h));
+    for (int h = 0; h < 10; ++h) {
+        if (d.ns_homo[h] <= 0) continue;
+        const int ci = (int)cs.size();
+        cs.push_back({d.ns_homo[h], h, h, d.ns_homo[h], SCFT_INIT_ONES, 0});
+        blocks.push_back({ci, ci, 0, d.ns_homo[h] - 1, d.ns_homo[h], 4 + h, h, 1});
+        c->species_h[4 + h] = {1, ci, d.ns_homo[h], 0};
+    }
+    for (int k = 0; k < 4; ++k) {
+        if (!(s.vol_dbk[k] > 0.0)) continue;
+        const int fx = DBK_FX[k], fy = fx + 1, ns = d.ns_dbk[k], nx_ = d.ns_dbk_x[k], ny_ = d.ns_dbk_y[k];
+        const int cf = (int)cs.size();
+        cs.push_back({ns, fx, fy, nx_ - 1, (k == 0 && s.enable_seed == 1) ? SCFT_INIT_SEED : SCFT_INIT_ONES, 0});
+        const int cb = (int)cs.size();
+        cs.push_back({ns, fy, fx, ny_, SCFT_INIT_ONES, 0});
+        blocks.push_back({cf, cb, 0, nx_ - 1, ns, k, fx, 0});
+        blocks.push_back({cf, cb, nx_ - 1, ns - 1, ns, k, fy, 0});
+        /* Q from the complementary chain for dbk1/2, the forward chain for dbk3/4 (SCFT.c:1271, :1314, :1357, :1399) */
+        c->species_h[k] = {1, k < 2 ? cb : cf, ns, 0};
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (d.ns_s[k] <= 0) continue;
+        const int ns = d.ns_s[k];
+        const int cf = (int)cs.size();
+        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_MASK, k});
+        const int cb = (int)cs.size();
+        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_ONES, 0});
+        blocks.push_back({cf, cb, 0, ns - 1, ns, 14 + k, 10 + k, 0});
+        c->species_h[14 + k] = {1, cf, ns, 0};
+    }
+    if (cs.empty()) {
+        set_err("no species with a positive volume fraction");
+        scft_ctx_destroy(c);
+        return SCFT_ERR_PARAM;
+    }
+    c->nchains = (int)cs.size();
+    c->nblocks = (int)blocks.size();
+    c->blocks_h = blocks;
+    c->maxlen = 0;
+    c->field_use = 0;
+    for (const ChainSpec &x : cs) {
+        if (x.len > c->maxlen) c->maxlen = x.len;
+        c->field_use |= 1u << x.f0;
+        c->field_use |= 1u << x.f1;
+    }
+
+    int rc = SCFT_OK;
+    const long sm = c->sm;
+    const int B = c->B;
+    void *p = nullptr;
+#define ALLOC(ptr, bytes)                                    \
+    do {                                                     \
+        rc = dalloc(c, &p, (bytes));                         \
+        if (rc) {                                            \
+            scft_ctx_destroy(c);                             \
+            return rc;                                       \
+        }                                                    \
+        ptr = (decltype(ptr))p;                              \
+    } while (0)
+    ALLOC(c->w, sizeof(double) * B * 14 * sm);
+    ALLOC(c->phi, sizeof(double) * B * 14 * sm);
+    ALLOC(c->raw, sizeof(double) * B * c->nblocks * sm);
+    ALLOC(c->mask, sizeof(double) * B * 3 * sm);
+    ALLOC(c->bz, (size_t)c->psize * B * SCFT_NFIELDS * sm);
+    c->nparts = scft_post_nparts(c->m, c->sms);
+    ALLOC(c->partial, sizeof(double) * B * SCFT_NSPECIES * c->nparts);
+    ALLOC(c->noise, sizeof(double) * B * d.n_active * sm);
+    c->hist_cap = 256;
+    ALLOC(c->hist, sizeof(scft_iter_out) * c->hist_cap * B);
+    if (cudaMallocHost((void **)&c->hist_host, sizeof(scft_iter_out) * c->hist_cap * B) != cudaSuccess) {
+        set_err("cudaMallocHost failed");
+        scft_ctx_destroy(c);
+        return SCFT_ERR_OOM;
+    }
+    c->chains_h.resize((size_t)B * c->nchains);
+    for (int b = 0; b < B; ++b)
+        for (int k = 0; k < c->nchains; ++k) {
+            const ChainSpec &x = cs[k];
+            ChainDesc &cd = c->chains_h[(size_t)b * c->nchains + k];
+            void *q, *t;
+            ALLOC(q, (size_t)c->psize * x.len * sm);
+            ALLOC(t, (size_t)c->psize * sm);
+            cd.q = q;
+            cd.tmp = t;
+            cd.b0 = (char *)c->bz + (size_t)c->psize * ((size_t)b * SCFT_NFIELDS + x.f0) * sm;
+            cd.b1 = (char *)c->bz + (size_t)c->psize * ((size_t)b * SCFT_NFIELDS + x.f1) * sm;
+            cd.seg_end = x.seg_end;
+            cd.len = x.len;
+            cd.init = x.init;
+            cd.init_arg = x.init_arg;
+            cd.instance = b;
+            cd.pad = 0;
+        }
+    std::vector<InstParams> ip(B);
+    for (int b = 0; b < B; ++b) fill_params(c->surf[b], c->der[b], c->blocks_h, c->species_h, ip[b]);
+    if ((rc = upload(c, (void **)&c->params, ip)) || (rc = upload(c, (void **)&c->chains, c->chains_h)) ||
+        (rc = upload(c, (void **)&c->blocks, c->blocks_h))) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
+    std::vector<SpeciesDesc> spv(c->species_h, c->species_h + SCFT_NSPECIES);
+    if ((rc = upload(c, (void **)&c->species, spv))) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
+    ALLOC(c->state, sizeof(InstState) * B);
+#undef ALLOC
+    if ((rc = build_axes(c))) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
+    c->iter.assign(B, 0);
+    c->rng.assign(3 * B, 0);
+    c->fields_set.assign(B, 0);
+    c->prop_launches_per_iter = (long)(c->maxlen - 1) * (long)c->axes.size();
+    c->launches_per_iter = c->prop_launches_per_iter + 2 + 6;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+        scft_ctx_destroy(c);
+        return SCFT_ERR_CUDA;
+    }
+    *out = c;
+    return SCFT_OK;
+}
+
+extern "C" int scft_ctx_derived(const scft_ctx *c, int b, scft_derived *d)
+{
+    if (!c || !d || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    *d = c->der[b];
+    return SCFT_OK;
+}
+
+extern "C" size_t scft_ctx_device_bytes(const scft_ctx *c) { return c ? c->device_bytes : 0; }
+
+extern "C" int scft_set_fields(scft_ctx *c, int b, const double *w14)
+{
+    if (!c || !w14 || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    for (int f = 0; f < 14; ++f)
+        CK(cudaMemcpyAsync(c->w + ((size_t)b * 14 + f) * c->sm, w14 + (size_t)f * c->m, sizeof(double) * c->m,
+                           cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->fields_set[b] = 1;
+    return SCFT_OK;
+}
+
+extern "C" int scft_set_masks(scft_ctx *c, int b, const double *mask3)
+{
+    if (!c || !mask3 || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    for (int f = 0; f < 3; ++f)
+        CK(cudaMemcpyAsync(c->mask + ((size_t)b * 3 + f) * c->sm, mask3 + (size_t)f * c->m, sizeof(double) * c->m,
+                           cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_set_iteration(scft_ctx *c, int b, unsigned long it)
+{
+    if (!c || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    c->iter[b] = it;
+    CK(cudaMemcpyAsync(&c->state[b].iter, &c->iter[b], sizeof(unsigned long), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_set_rng(scft_ctx *c, int b, const unsigned short seed[3])
+{
+    if (!c || !seed || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    memcpy(&c->rng[3 * b], seed, 3 * sizeof(unsigned short));
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_rng(const scft_ctx *c, int b, unsigned short seed[3])
+{
+    if (!c || !seed || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    memcpy(seed, &c->rng[3 * b], 3 * sizeof(unsigned short));
+    return SCFT_OK;
+}
+
+static PostArgs post_args(scft_ctx *c, const double *noise_dev)
+{
+    PostArgs a;
+    memset(&a, 0, sizeof(a));
+    a.params = c->params;
+    a.state = c->state;
+    a.chains = c->chains;
+    a.blocks = c->blocks;
+    a.species = c->species;
+    a.nchains = c->nchains;
+    a.nblocks = c->nblocks;
+    a.B = c->B;
+    a.nx = c->nx;
+    a.ny = c->ny;
+    a.nz = c->nz;
+    a.m = c->m;
+    a.sm = c->sm;
+    a.w = c->w;
+    a.phi = c->phi;
+    a.raw = c->raw;
+    a.mask = c->mask;
+    a.bz = c->bz;
+    a.field_use = c->field_use;
+    a.partial = c->partial;
+    a.nparts = c->nparts;
+    a.noise = noise_dev;
+    a.hist = c->hist;
+    a.hist_cap = c->hist_cap;
+    return a;
+}
+
+/* All contour steps of every chain: one launch per axis per step. */
+static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total, int maxlen)
+{
+    const int npass = (int)c->axes.size();
+    for (int s = 0; s < maxlen - 1; ++s) {
+        for (int pi = 0; pi < npass; ++pi) {
+            const Axis &A = c->axes[pi];
+            PassArgs pa;
+            memset(&pa, 0, sizeof(pa));
+            pa.chains = chains;
+            pa.nchains = nchains_total;
+            pa.s = s;
+            pa.first = pi == 0;
+            pa.last = pi == npass - 1;
+            pa.tile = A.tile;
+            pa.sstride = c->sm;
+            pa.spec = A.spec;
+            pa.tw = A.tw;
+            pa.kA = A.kA;
+            pa.kB = A.kB;
+            pa.h = A.h;
+            pa.even = A.even;
+            CK(scft_launch_pass(c->opt.precision, A.g, pa, A.ntiles, c->stream));
+        }
+    }
+    return SCFT_OK;
+}
+
+static int launch_iteration(scft_ctx *c, const double *noise_dev, int slot)
+{
+    PostArgs a = post_args(c, noise_dev);
+    if (c->timing) CK(cudaEventRecord(c->ev[2 + 2 * slot], c->stream));
+    CK(scft_post_iter_begin(a, c->opt.precision, c->sms, c->stream));
+    int rc = launch_steps(c, c->chains, c->B * c->nchains, c->maxlen);
+    if (rc) return rc;
+    if (c->timing) CK(cudaEventRecord(c->ev[3 + 2 * slot], c->stream));
+    CK(scft_post_iter_end(a, c->opt.precision, c->sms, c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_out *out)
+{
+    if (!c || n < 0) return SCFT_ERR_PARAM;
+    for (int b = 0; b < c->B; ++b)
+        if (!c->fields_set[b]) {
+            set_err("instance %d: scft_set_fields was not called", b);
+            return SCFT_ERR_STATE;
+        }
+    cudaSetDevice(c->device);
+    if (!noise) {
+        /* without noise arrays every iteration must have MF*DT_NOISE == 0 */
+        for (int b = 0; b < c->B; ++b)
+            for (int k = 1; k <= n; ++k) {
+                const unsigned long it = c->iter[b] + k;
+                const double mf = it > (unsigned long)c->surf[b].relaxation ? 0.0 : 1.0;
+                if (mf * c->surf[b].dt_noise != 0.0) {
+                    set_err("iteration %lu of instance %d adds noise but no noise arrays were passed", it, b);
+                    return SCFT_ERR_PARAM;
+                }
+            }
+    }
+    if (c->timing && c->ev.empty()) {
+        c->ev.resize(2 + 2 * c->hist_cap);
+        for (cudaEvent_t &e : c->ev) CK(cudaEventCreate(&e));
+    }
+    c->last_timing = scft_timing{};
+    int done = 0;
+    while (done < n) {
+        const int chunk = (n - done) < c->hist_cap ? (n - done) : c->hist_cap;
+        PostArgs a = post_args(c, nullptr);
+        CK(scft_post_mark_start(a, c->stream));
+        if (c->timing) CK(cudaEventRecord(c->ev[0], c->stream));
+        for (int k = 0; k < chunk; ++k) {
+            const double *nd = nullptr;
+            if (noise) {
+                const size_t m = (size_t)c->m, na = c->der[0].n_active;
+                for (int b = 0; b < c->B; ++b)
+                    for (size_t f = 0; f < na; ++f)
+                        CK(cudaMemcpyAsync(c->noise + ((size_t)b * na + f) * c->sm,
+                                           noise + ((size_t)(done + k) * c->B * na + (size_t)b * na + f) * m,
+                                           sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
+                nd = c->noise;
+            }
+            if (c->opt.use_graph && !c->timing) {
+                if (!c->graph_exec) {
+                    /* the graph always reads noise from c->noise; with no noise the
+                     * buffer holds zeros and MF*DT_NOISE == 0 skips it */
+                    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                    int rc = launch_iteration(c, c->noise, k);
+                    cudaGraph_t g = nullptr;
+                    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                    if (rc) return rc;
+                    CK(e);
+                    c->graph = g;
+                    CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
+                }
+                CK(cudaGraphLaunch(c->graph_exec, c->stream));
+            } else {
+                int rc = launch_iteration(c, nd, k);
+                if (rc) return rc;
+            }
+        }
+        if (c->timing) CK(cudaEventRecord(c->ev[1], c->stream));
+        CK(cudaMemcpyAsync(c->hist_host, c->hist, sizeof(scft_iter_out) * chunk * c->B, cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->timing) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+            c->last_timing.total_ms += ms;
+            for (int k = 0; k < chunk; ++k) {
+                float pm = 0.f;
+                cudaEventElapsedTime(&pm, c->ev[2 + 2 * k], c->ev[3 + 2 * k]);
+                c->last_timing.prop_ms += pm;
+            }
+        }
+        c->last_timing.prop_launches += (long)chunk * c->prop_launches_per_iter;
+        c->last_timing.kernel_launches += (long)chunk * c->launches_per_iter;
+        int status = SCFT_OK;
+        for (int k = 0; k < chunk; ++k)
+            for (int b = 0; b < c->B; ++b) {
+                const scft_iter_out &r = c->hist_host[(size_t)k * c->B + b];
+                if (out) out[(size_t)(done + k) * c->B + b] = r;
+                if (r.status != SCFT_OK) status = r.status;
+            }
+        for (int b = 0; b < c->B; ++b) c->iter[b] += chunk;
+        done += chunk;
+        if (status != SCFT_OK) {
+            set_err("non-finite Q, free energy or RMS");
+            return status;
+        }
+    }
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_fields(scft_ctx *c, int b, double *w14)
+{
+    if (!c || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    if (!w14) return SCFT_OK;
+    cudaSetDevice(c->device);
+    for (int f = 0; f < 14; ++f)
+        CK(cudaMemcpyAsync(w14 + (size_t)f * c->m, c->w + ((size_t)b * 14 + f) * c->sm, sizeof(double) * c->m,
+                           cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_densities(scft_ctx *c, int b, double *phi13, double *phi_tot)
+{
+    if (!c || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    if (phi13)
+        for (int f = 0; f < 13; ++f)
+            CK(cudaMemcpyAsync(phi13 + (size_t)f * c->m, c->phi + ((size_t)b * 14 + f) * c->sm, sizeof(double) * c->m,
+                               cudaMemcpyDeviceToHost, c->stream));
+    if (phi_tot)
+        CK(cudaMemcpyAsync(phi_tot, c->phi + ((size_t)b * 14 + 13) * c->sm, sizeof(double) * c->m,
+                           cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_propagate(scft_ctx *c, const double *q0, const double *w, int steps, double *q_out)
+{
+    if (!c || !q0 || !w || !q_out || steps < 0) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    const size_t sm = c->sm, m = c->m;
+    double *wd = nullptr, *qd = nullptr;
+    void *q = nullptr, *tmp = nullptr, *bzd = nullptr;
+    ChainDesc *cdd = nullptr;
+    int rc = SCFT_OK;
+    cudaError_t e = cudaSuccess;
+    e = cudaMalloc(&wd, sizeof(double) * sm);
+    if (e == cudaSuccess) e = cudaMalloc(&qd, sizeof(double) * sm * (steps + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&q, (size_t)c->psize * sm * (steps + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, (size_t)c->psize * sm);
+    if (e == cudaSuccess) e = cudaMalloc(&bzd, (size_t)c->psize * sm);
+    if (e == cudaSuccess) e = cudaMalloc(&cdd, sizeof(ChainDesc));
+    if (e != cudaSuccess) {
+        set_err("scft_propagate: allocation failed: %s", cudaGetErrorString(e));
+        rc = SCFT_ERR_OOM;
+    }
+    if (rc == SCFT_OK) {
+        ChainDesc cd;
+        memset(&cd, 0, sizeof(cd));
+        cd.q = q;
+        cd.tmp = tmp;
+        cd.b0 = bzd;
+        cd.b1 = bzd;
+        cd.seg_end = steps + 1;
+        cd.len = steps + 1;
+        e = cudaMemcpyAsync(cdd, &cd, sizeof(cd), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(wd, w, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(qd, q0, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = scft_boltz_one(c->opt.precision, wd, bzd, c->der[0].ds, (long)m, c->stream);
+        if (e == cudaSuccess) e = scft_convert(c->opt.precision, qd, q, (long)m, 1, c->stream);
+        if (e != cudaSuccess) {
+            set_err("scft_propagate: %s", cudaGetErrorString(e));
+            rc = SCFT_ERR_CUDA;
+        }
+    }
+    if (rc == SCFT_OK) rc = launch_steps(c, cdd, 1, steps + 1);
+    if (rc == SCFT_OK) {
+        e = scft_convert(c->opt.precision, (const double *)q, qd, (long)(sm * (steps + 1)), 0, c->stream);
+        for (int s = 0; s <= steps && e == cudaSuccess; ++s)
+            e = cudaMemcpyAsync(q_out + (size_t)s * m, qd + (size_t)s * sm, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                                c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            set_err("scft_propagate: %s", cudaGetErrorString(e));
+            rc = SCFT_ERR_CUDA;
+        }
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(wd);
+    cudaFree(qd);
+    cudaFree(q);
+    cudaFree(tmp);
+    cudaFree(bzd);
+    cudaFree(cdd);
+    return rc;
+}
+
+extern "C" int scft_enable_timing(scft_ctx *c, int on)
+{
+    if (!c) return SCFT_ERR_PARAM;
+    c->timing = on ? 1 : 0;
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
+{
+    if (!c || !t) return SCFT_ERR_PARAM;
+    *t = c->last_timing;
+    return SCFT_OK;
+}

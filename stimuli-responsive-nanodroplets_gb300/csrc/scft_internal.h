@@ -1,0 +1,150 @@
+/*
+ * scft_internal.h — device-side layout of one SCFT context (not part of the ABI).
+ *
+ * HBM layout per context (B instances that share grid and contour counts):
+ *   fields   w[b][14][SM]      FP64: 13 chemical potentials + pressure p
+ *   boltz    bz[b][13][SM]     P: exp(-DS*w/2) per field (SCFT.c:2344)
+ *   masks    mk[b][3][SM]      FP64: brush grafting masks (wMask.dat)
+ *   q        per chain c: q_c[s][SM] P, s = 0..len-1 (contour-major SoA; the
+ *            reference is AoS q[s + NS*idx], SCFT.c:2398)
+ *   tmp      per chain c: one slice, the intermediate of a multi-pass step
+ *   raw      raw[b][block][SM] FP64: unnormalised Simpson sums per density block
+ *   phi      phi[b][14][SM] FP64: 13 total densities + phi_tot
+ * SM is M rounded up to a multiple of 64 elements so every slice starts on a
+ * 512-byte boundary.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "scft_gpu.h"
+
+#define SCFT_MAX_CHAINS 26  /* 10 homo + 4*2 dbk + 3*2 brush */
+#define SCFT_MAX_BLOCKS 21  /* 10 homo + 4*2 dbk + 3 brush */
+#define SCFT_MAX_RADIX_STAGES 12
+#define SCFT_INIT_ONES 0
+#define SCFT_INIT_MASK 1
+#define SCFT_INIT_SEED 2
+
+/* One propagator chain of one instance: q[0] from init, then len-1 contour
+ * steps; steps s < seg_end use field f0, later steps field f1 (the diblock
+ * junction). */
+struct ChainDesc {
+    void *q;        /* len slices */
+    void *tmp;      /* one slice */
+    const void *b0; /* Boltzmann factor slice of f0 */
+    const void *b1; /* ... of f1 */
+    int seg_end;
+    int len;
+    int init;       /* SCFT_INIT_* */
+    int init_arg;   /* mask index for SCFT_INIT_MASK */
+    int instance;
+    int pad;
+};
+
+/* One funDensity call (SCFT.c:2270-2308) of one species block. */
+struct BlockDesc {
+    int chain_f;   /* forward propagator chain (index within the instance) */
+    int chain_b;   /* complementary chain (== chain_f for homopolymers) */
+    int start, stop;
+    int len;       /* NS_EFF of the species */
+    int species;   /* 0..16: which Q normalises it */
+    int field;     /* 0..12: which total it adds to */
+    int part;      /* 0: first operand of funAddArray (diblock/brush), 1: second (homo) */
+};
+
+/* Species whose Q comes from chain q_chain at slice len-1 (SCFT.c:1837-1872). */
+struct SpeciesDesc {
+    int present;
+    int q_chain;
+    int len;
+    int pad;
+};
+
+/* Per-instance scalars read by the fused update kernel. */
+struct InstParams {
+    double chi[SCFT_NFIELDS][SCFT_NFIELDS];
+    double phi_avg[SCFT_NFIELDS];
+    double frac[SCFT_MAX_BLOCKS];        /* funVolFrac factor per block */
+    double lnq_coef[SCFT_NSPECIES];      /* H_fe_fraction coefficient per species */
+    double g1, g2, dt_noise, ds;
+    long relaxation;
+    int active[SCFT_NFIELDS];
+    int n_active;
+    int enable_seed, seed_steps, seed_area_delta;
+    int mask;
+    int pad;
+};
+
+/* Per-instance device state that changes every iteration. */
+struct InstState {
+    unsigned long iter;   /* iIter, incremented at the start of each iteration */
+    unsigned long iter0;  /* value at the start of the current scft_iterate call */
+    double q[SCFT_NSPECIES];
+    double p_avg;
+    int status;
+    int pad;
+};
+
+/* Geometry of one axis pass of the propagator step. */
+struct AxisGeom {
+    int n;         /* line length */
+    int ls;        /* element stride along the line */
+    int inner;     /* lines per outer group sharing a base (x, y axes) */
+    int outer;     /* number of outer groups */
+    int dirichlet; /* 1: dense Dirichlet operator, 0: periodic FFT */
+    int nrad;
+    int rad[SCFT_MAX_RADIX_STAGES];
+};
+
+/* Arguments of one axis pass of the propagator step (scft_prop.cu). */
+struct PassArgs {
+    const ChainDesc *chains;
+    int nchains;
+    int s;          /* contour step: reads slice s, writes slice s+1 */
+    int first;      /* multiply by b on load, read q[s] */
+    int last;       /* multiply by b on store, write q[s+1] */
+    int tile;       /* lines per CTA */
+    long sstride;   /* slice stride (elements) */
+    const void *spec; /* P[n]: E(k_t)/n (periodic) */
+    const void *tw;   /* Cx<P>[n] twiddles (periodic) */
+    const void *kA;   /* P[h*h] transposed, dense Dirichlet half operators */
+    const void *kB;
+    int h;          /* half size (n even) or n (odd: kA holds the full matrix) */
+    int even;
+};
+
+size_t scft_pass_smem_bytes(const AxisGeom &g, int tile, int h, int psize);
+cudaError_t scft_pass_configure(int smem_bytes);
+cudaError_t scft_launch_pass(int prec, const AxisGeom &g, const PassArgs &a, int ntiles, cudaStream_t st);
+
+/* Arguments shared by the non-propagator kernels (scft_post.cu). */
+struct PostArgs {
+    const InstParams *params;   /* [B] */
+    InstState *state;           /* [B] */
+    const ChainDesc *chains;    /* [B * nchains] */
+    const BlockDesc *blocks;    /* [nblocks] (same for every instance) */
+    const SpeciesDesc *species; /* [17] */
+    int nchains, nblocks;
+    int B;
+    int nx, ny, nz;
+    long m, sm;                 /* points, slice stride */
+    double *w;                  /* [B][14][sm] */
+    double *phi;                /* [B][14][sm]: 13 totals + phi_tot */
+    double *raw;                /* [B][nblocks][sm] */
+    const double *mask;         /* [B][3][sm] */
+    void *bz;                   /* [B][13][sm] P */
+    unsigned field_use;         /* bit f: some chain propagates with field f */
+    double *partial;            /* [B][nparts][...] */
+    int nparts;
+    const double *noise;        /* [B][n_active][sm] or NULL */
+    scft_iter_out *hist;        /* [cap][B] */
+    int hist_cap;
+};
+
+cudaError_t scft_post_iter_begin(const PostArgs &a, int prec, int sms, cudaStream_t st);
+cudaError_t scft_post_mark_start(const PostArgs &a, cudaStream_t st);
+cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_t st);
+int scft_post_nparts(long m, int sms);
+cudaError_t scft_convert(int prec, const double *src, void *dst, long n, int to_p, cudaStream_t st);
+cudaError_t scft_boltz_one(int prec, const double *w, void *bz, double ds, long m, cudaStream_t st);
