@@ -1,0 +1,385 @@
+"""Benchmark: SCFT iterations/s of the thin-film nanodroplet system on one GB300.
+
+Workload (default): the droplet system of the 2D thin-film configuration
+(MASK 1, grid 192x1x96, NS = 128: AB diblock f = 0.5 at VOL 0.20, homopolymer C
+solvent, brush S1 at z = 0; 502 contour steps per iteration), as a phase-diagram
+batch of B instances on a chi_AB N x chi_AC N sweep, each started from a seeded
+half-disk droplet. A step is one SCFT iteration of every instance.
+
+value     instance-iterations/s of the FP32-propagator / FP64-reduction form,
+          inputs resident in HBM, CUDA events on the library's stream.
+e2e       the same through the C ABI with host buffers: per step the restart
+          fields of every instance go host->device (pinned), one iteration
+          runs, fields and densities come back device->host.
+fp64_plain  the plain FP64 form (the drop-in) on the same batch.
+roofline  propagator passes: algorithmic bytes 3*P*M per contour step per
+          chain (read q_s, read exp(-w ds/2), write q_{s+1}) over the time of the
+          propagator launches.
+cpu_baseline  the CPU restatement of SCFT.c (oracle/, same algorithm, data
+          layout and FFT code as the reference built here) on the host cores,
+          one instance per core, bounded sample.
+
+--impl reference times that CPU implementation alone on the same workload.
+Under torchrun every rank runs its own batch (replicas: SCFT solves are
+independent, there is no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+PKG = "stimuli-responsive-nanodroplets_gb300"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+TRAFFIC = ROOT / "profiles" / "traffic.json"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload_surfaces(srn, name: str, batch: int):
+    n = int(round(np.sqrt(batch)))
+    out = []
+    for b in range(batch):
+        a, c = divmod(b, max(n, 1))
+        chi_ab = 10.0 + 20.0 * (a % n) / max(n - 1, 1)
+        chi_ac = 20.0 + 40.0 * c / max(n - 1, 1)
+        if name == "film2d":
+            out.append(srn.configs.film2d(chi_ab=chi_ab, chi_ac=chi_ac))
+        elif name == "bulk2d":
+            s = srn.configs.bulk2d()
+            s.set_chi("A", "B", chi_ab)
+            out.append(s)
+        else:
+            raise SystemExit(f"unknown workload {name}")
+    return out
+
+
+def initial_fields(srn, s, seed):
+    if s.MASK:
+        return srn.configs.droplet_fields(s, seed=seed), srn.configs.substrate_mask(s)
+    return srn.configs.uniform_fields(s.grid(), seed=seed, amp=0.1), None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            v = [x.strip() for x in line.split(",")]
+            if len(v) == 7:
+                self.rows.append(v)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(solver, psize: int) -> float:
+    """Sum over chains of (len-1) contour steps x 3*P*M, per instance-iteration."""
+    d = solver.derived[0]
+    steps = 0
+    for k in range(4):
+        if d.ns_dbk[k] > 0:
+            steps += 2 * (int(d.ns_dbk[k]) - 1)
+    for h in range(10):
+        if d.ns_homo[h] > 0:
+            steps += int(d.ns_homo[h]) - 1
+    for k in range(3):
+        if d.ns_s[k] > 0:
+            steps += 2 * (int(d.ns_s[k]) - 1)
+    return float(steps) * 3 * psize * solver.M, steps
+
+
+def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device: int, sync, e2e_steps: int):
+    B = len(surfaces)
+    sv = srn.Solver(surfaces, precision=precision, device=device)
+    init = [initial_fields(srn, s, 1000 + b) for b, s in enumerate(surfaces)]
+    for b, (w, m) in enumerate(init):
+        sv.set_fields(w, b)
+        if m is not None:
+            sv.set_masks(m, b)
+        sv.set_iteration(1, b)
+    sv.iterate(warmup)
+    sv.enable_timing(True)
+    sync()
+    t0 = time.perf_counter()
+    with ClockSampler(device) as clk:
+        outs = sv.iterate(steps)
+    wall = time.perf_counter() - t0
+    t = sv.timing()
+    sync()
+    bytes_iter, steps_iter = algorithmic_bytes(sv, 8 if precision == "fp64" else 4)
+    ms = t["total_ms"]
+    res = {
+        "value": B * steps / (ms * 1e-3),
+        "ms_per_step": ms / steps,
+        "wall_ms_per_step": wall * 1e3 / steps,
+        "prop_ms_per_step": t["prop_ms"] / steps,
+        "prop_launches_per_step": t["prop_launches"] / steps,
+        "gpu_launches": int(t["kernel_launches"]),
+        "clocks": clk.summary(),
+        "free_energy_first_instance": outs[-1][0].free_energy,
+        "algorithmic_bytes_per_step": bytes_iter * B,
+        "contour_steps_per_instance_iteration": steps_iter,
+        "device_bytes": sv.device_bytes,
+    }
+    res["achieved_gbs"] = bytes_iter * B / (t["prop_ms"] * 1e-3 / steps) / 1e9
+    # end to end through the C ABI with pinned host buffers
+    if e2e_steps > 0:
+        import torch
+        M = sv.M
+        w_host = [torch.empty((14, M), dtype=torch.float64, pin_memory=True).numpy() for _ in range(B)]
+        phi_host = [torch.empty((13, M), dtype=torch.float64, pin_memory=True).numpy() for _ in range(B)]
+        for b in range(B):
+            w_host[b][:] = sv.get_fields(b)
+        sv.enable_timing(False)
+        import ctypes as C
+        Lm = importlib.import_module(f"{PKG}._lib")
+        dp = C.POINTER(C.c_double)
+        lib = Lm.lib()
+        recs = (Lm.CIterOut * B)()
+        sync()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for b in range(B):
+                Lm.check(lib.scft_set_fields(sv._h, b, w_host[b].ctypes.data_as(dp)), "set_fields")
+            Lm.check(lib.scft_iterate(sv._h, 1, None, recs), "iterate")
+            for b in range(B):
+                Lm.check(lib.scft_get_fields(sv._h, b, w_host[b].ctypes.data_as(dp)), "get_fields")
+                Lm.check(lib.scft_get_densities(sv._h, b, phi_host[b].ctypes.data_as(dp), None), "get_densities")
+        sync()
+        e2e = time.perf_counter() - t0
+        res["e2e"] = {"value": B * e2e_steps / e2e, "unit": "instance-iterations/s",
+                      "h2d_bytes_per_step": B * 14 * M * 8,
+                      "d2h_bytes_per_step": B * (14 + 13) * M * 8 + B * C.sizeof(Lm.CIterOut)}
+    sv.close()
+    return res
+
+
+def cpu_sample(surfaces, threads: int, iters: int):
+    """The CPU restatement of SCFT.c, one instance per thread (ctypes drops the GIL)."""
+    srn = importlib.import_module(PKG)
+    from oracle.oracle import Oracle
+    work = []
+    for t in range(threads):
+        s = surfaces[t % len(surfaces)]
+        w, m = initial_fields(srn, s, 1000 + t)
+        o = Oracle(s)
+        o.set_fields(w)
+        if m is not None:
+            o.set_masks(m)
+        o.set_iter(1)
+        work.append(o)
+    times = [0.0] * threads
+
+    def go(k):
+        t0 = time.perf_counter()
+        work[k].iterate(iters)
+        times[k] = time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=go, args=(k,)) for k in range(threads)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    wall = time.perf_counter() - t0
+    for o in work:
+        o.close()
+    return threads * iters / wall, wall
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    srn = importlib.import_module(PKG)
+    surfaces = workload_surfaces(srn, args.workload, args.batch)
+    threads = args.cpu_threads or os.cpu_count() or 1
+    cpu_sample(surfaces, threads, 1) if args.warmup > 0 else None
+    rates = []
+    steps = min(args.steps, args.ref_max_steps)
+    t_all = 0.0
+    for _ in range(steps):
+        r, wall = cpu_sample(surfaces, threads, 1)
+        rates.append(r)
+        t_all += wall
+    value = threads * steps / t_all
+    line = {
+        "impl": "reference", "metric": "SCFT iterations/s", "value": value, "unit": "instance-iterations/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3 / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded droplet fields)",
+        "config": workload_config(args, surfaces),
+        "cpu_baseline": {"value": value, "unit": "instance-iterations/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} steps x 1 iteration of {threads} instances, one per host thread "
+                                   f"(SCFT.c's algorithm, data layout and FFT code restated "
+                                   f"in oracle/)"},
+        "e2e": {"value": value, "unit": "instance-iterations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, surfaces):
+    s = surfaces[0]
+    nx, ny, nz = s.grid()
+    return {"workload": f"{args.workload} {nx}x{ny}x{nz} NS={s.NS} MASK={s.MASK}, {len(surfaces)} instances "
+                        f"(chi_AB x chi_AC sweep), seeded droplet start",
+            "instances_per_gpu": len(surfaces), "grid": [nx, ny, nz], "ns": s.NS, "mask": s.MASK,
+            "l2": "working set larger than L2 (propagators of all instances)",
+            "parallelism": "replicas (one batch per GPU)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="film2d")
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--cpu-iters", type=int, default=1)
+    ap.add_argument("--ref-max-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one iteration of one form only (for ncu captures); prints no bench line")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    srn = importlib.import_module(PKG)
+    importlib.import_module(f"{PKG}.build").build()
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def sync():
+        torch.cuda.synchronize()
+        if pg is not None:
+            pg.barrier()
+
+    surfaces = workload_surfaces(srn, args.workload, args.batch)
+    if args.profile_case:
+        sv = srn.Solver(surfaces, precision=args.precision, device=local)
+        for b, s in enumerate(surfaces):
+            w, m = initial_fields(srn, s, 1000 + b)
+            sv.set_fields(w, b)
+            if m is not None:
+                sv.set_masks(m, b)
+            sv.set_iteration(1, b)
+        out = sv.iterate(1)
+        torch.cuda.synchronize()
+        print(f"profile case: {len(surfaces)} instances, F[0] = {out[0][0].free_energy:.12f}")
+        sv.close()
+        return
+    f32 = measure_form(srn, surfaces, "fp32", args.steps, args.warmup, local, sync, args.e2e_steps)
+    f64 = measure_form(srn, surfaces, "fp64", args.fp64_steps, 1, local, sync, 0)
+    ms = f32["ms_per_step"]
+    if pg is not None:
+        t = torch.tensor([ms, f64["ms_per_step"]], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms, ms64 = float(t[0]), float(t[1])
+    else:
+        ms64 = f64["ms_per_step"]
+    B = len(surfaces)
+    value = world * B / (ms * 1e-3)
+    peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    if TRAFFIC.exists():
+        traffic = json.loads(TRAFFIC.read_text()).get("fp32", {}).get("traffic_bytes_per_launch")
+    line = {
+        "metric": "SCFT iterations/s", "value": value, "unit": "instance-iterations/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 propagators, f64 densities/Q/free energy/update",
+        "data": "synthetic (seeded half-disk droplet fields, chi sweep)",
+        "config": workload_config(args, surfaces),
+        "e2e": f32.get("e2e"),
+        "gpu_launches": f32["gpu_launches"],
+        "clocks": f32["clocks"],
+        "roofline": {"bound": "hbm", "achieved": f32["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": f32["achieved_gbs"] / peak, "traffic": traffic,
+                     "peak_source": "measured" if PEAKS.exists() else "fallback",
+                     "kernel": "propagator passes (k_pass_fft + k_pass_dense)",
+                     "algorithmic_bytes_per_launch": f32["algorithmic_bytes_per_step"] / f32["prop_launches_per_step"],
+                     "launch_ms": f32["prop_ms_per_step"] / f32["prop_launches_per_step"]},
+        "fp64_plain": {"value": world * B / (ms64 * 1e-3), "ms_per_step": ms64, "steps": args.fp64_steps,
+                       "achieved_gbs": f64["achieved_gbs"], "frac": f64["achieved_gbs"] / peak,
+                       "prop_ms_per_step": f64["prop_ms_per_step"], "clocks": f64["clocks"]},
+        "detail": {"fp32_prop_ms_per_step": f32["prop_ms_per_step"], "fp32_wall_ms_per_step": f32["wall_ms_per_step"],
+                   "contour_steps_per_instance_iteration": f32["contour_steps_per_instance_iteration"],
+                   "device_bytes_fp32": f32["device_bytes"]},
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = args.cpu_threads or os.cpu_count() or 1
+        rate, wall = cpu_sample(surfaces, threads, args.cpu_iters)
+        line["cpu_baseline"] = {"value": rate, "unit": "instance-iterations/s", "cores": threads, "kind": "port",
+                                "sample": f"{args.cpu_iters} iteration(s) of {threads} instances, one per host "
+                                          f"thread, {wall:.1f} s (SCFT.c's algorithm restated in oracle/)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
