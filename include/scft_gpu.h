@@ -106,7 +106,9 @@ typedef struct scft_options {
     int noise_mode;  /* SCFT_NOISE_* */
     int use_graph;   /* capture one iteration as a CUDA graph and replay it */
     int n_instances; /* instances in this context (batching form); 1 for a single solve */
-    int reserved[3];
+    int kernel_path; /* 0: fused single-launch contour step where the shape has one, else per-axis
+                        passes; 1: per-axis passes only */
+    int reserved[2];
 } scft_options;
 
 void scft_options_default(scft_options *o);

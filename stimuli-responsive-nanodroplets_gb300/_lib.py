@@ -85,7 +85,7 @@ class CDerived(C.Structure):
 
 class COptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("noise_mode", C.c_int), ("use_graph", C.c_int),
-                ("n_instances", C.c_int), ("reserved", C.c_int * 3)]
+                ("n_instances", C.c_int), ("kernel_path", C.c_int), ("reserved", C.c_int * 2)]
 
 
 class CIterOut(C.Structure):

@@ -16,6 +16,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "scft_internal.h"
@@ -66,6 +67,10 @@ struct scft_ctx {
     std::vector<BlockDesc> blocks_h;
     SpeciesDesc species_h[SCFT_NSPECIES];
     std::vector<Axis> axes;
+    /* fused 2D contour step (scft_step2d.cu) */
+    int fused2d = 0;
+    void *kz_rm = nullptr, *twx = nullptr, *ex = nullptr;
+    int *order = nullptr; /* chain indices, longest first */
     /* device memory */
     double *w = nullptr, *phi = nullptr, *raw = nullptr, *mask = nullptr, *partial = nullptr, *noise = nullptr;
     void *bz = nullptr;
@@ -204,12 +209,100 @@ static int upload_p(scft_ctx *c, void **dst, const std::vector<double> &v)
     return upload(c, dst, f);
 }
 
+/* Round an n x n operator block (row-major) to FP32 so that every column sum of
+ * the FP32 values equals the FP64 column sum as closely as FP32 allows: each
+ * entry is first rounded to nearest, then the residual of its column is handed
+ * out in steps of one ulp, largest entries first, each entry moving by at most
+ * one ulp. The mean mode of q passes through 1^T A only, so this keeps the FP32
+ * step free of a systematic per-step gain that would otherwise add up over a
+ * chain's contour steps (and bias ln Q). */
+static std::vector<double> round_fp32_colsum(const std::vector<double> &A, int rows, int cols)
+{
+    std::vector<double> out(A.size());
+    std::vector<int> order(rows);
+    for (int k = 0; k < cols; ++k) {
+        long double target = 0.0L, have = 0.0L;
+        for (int i = 0; i < rows; ++i) {
+            const float r = (float)A[(size_t)i * cols + k];
+            out[(size_t)i * cols + k] = r;
+            target += (long double)A[(size_t)i * cols + k];
+            have += (long double)r;
+        }
+        for (int i = 0; i < rows; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) {
+            return fabs(A[(size_t)x * cols + k]) > fabs(A[(size_t)y * cols + k]);
+        });
+        long double resid = target - have;
+        for (int t = 0; t < rows && resid != 0.0L; ++t) {
+            const int i = order[t];
+            const float r = (float)out[(size_t)i * cols + k];
+            if (r == 0.0f) continue;
+            const float up = nextafterf(r, INFINITY), dn = nextafterf(r, -INFINITY);
+            const long double ulp_up = (long double)up - r, ulp_dn = (long double)r - dn;
+            if (resid >= ulp_up / 2) {
+                out[(size_t)i * cols + k] = up;
+                resid -= ulp_up;
+            } else if (-resid >= ulp_dn / 2) {
+                out[(size_t)i * cols + k] = dn;
+                resid += ulp_dn;
+            }
+        }
+    }
+    return out;
+}
+
 static int pick_tile(long lines_per_chain, long inner_or_lines, int total_chains, int sms, int start)
 {
     int tile = start;
     while (tile > 2 && (inner_or_lines % tile != 0 || (lines_per_chain / tile) * (long)total_chains < 2L * sms)) tile /= 2;
     while (tile > 1 && inner_or_lines % tile != 0) tile /= 2;
     return tile;
+}
+
+/* The fused 2D step: z operator rows (A then B, row-major), the four-step
+ * twiddles along x and the x factor E(k)/NX. */
+static int build_fused2d(scft_ctx *c)
+{
+    const scft_derived &d = c->der[0];
+    if (c->opt.kernel_path != 0 || d.ny != 1 || d.nx < 2 || d.nz < 2) return SCFT_OK;
+    if (scft_step2d_smem(c->opt.precision, d.nx, d.nz) == 0) return SCFT_OK;
+    const int nz = d.nz, h = nz / 2, nx = d.nx, n1 = scft_step2d_n1(nx), n2 = nx / n1;
+    std::vector<long double> K;
+    dense_operator(nz, d.alphaz, c->surf[0].mask, K);
+    std::vector<double> kz((size_t)2 * h * h);
+    for (int i = 0; i < h; ++i)
+        for (int j = 0; j < h; ++j) {
+            const long double kij = K[(size_t)i * nz + j], kim = K[(size_t)i * nz + (nz - 1 - j)];
+            kz[(size_t)i * h + j] = (double)((kij + kim) / 2.0L);
+            kz[(size_t)h * h + (size_t)i * h + j] = (double)((kij - kim) / 2.0L);
+        }
+    if (c->psize == 4) {
+        std::vector<double> Ah(kz.begin(), kz.begin() + (size_t)h * h), Bh(kz.begin() + (size_t)h * h, kz.end());
+        Ah = round_fp32_colsum(Ah, h, h);
+        Bh = round_fp32_colsum(Bh, h, h);
+        std::copy(Ah.begin(), Ah.end(), kz.begin());
+        std::copy(Bh.begin(), Bh.end(), kz.begin() + (size_t)h * h);
+    }
+    std::vector<double> twx(2 * (size_t)nx), ex(nx);
+    for (int q2 = 0; q2 < n2; ++q2)
+        for (int k1 = 0; k1 < n1; ++k1) {
+            const double ang = 2.0 * M_PI * (double)((q2 * k1) % nx) / nx;
+            twx[2 * (q2 * n1 + k1)] = cos(ang);
+            twx[2 * (q2 * n1 + k1) + 1] = -sin(ang);
+        }
+    for (int k = 0; k < nx; ++k) {
+        const double kk = kval(k, nx);
+        ex[k] = exp(-d.alphax * kk * kk) / nx;
+    }
+    int rc = upload_p(c, &c->kz_rm, kz);
+    if (!rc) rc = upload_p(c, &c->twx, twx);
+    if (!rc) rc = upload_p(c, &c->ex, ex);
+    if (rc) return rc;
+    Step2DArgs a;
+    memset(&a, 0, sizeof(a));
+    CK(scft_launch_step2d(c->opt.precision, nx, nz, a, 0, c->stream, 1));
+    c->fused2d = 1;
+    return SCFT_OK;
 }
 
 static int build_axes(scft_ctx *c)
@@ -252,12 +345,21 @@ static int build_axes(scft_ctx *c)
             if (A.even) {
                 const int h = n / 2;
                 A.h = h;
-                std::vector<double> At((size_t)h * h), Bt((size_t)h * h);
+                std::vector<double> Ar((size_t)h * h), Br((size_t)h * h), At((size_t)h * h), Bt((size_t)h * h);
                 for (int i = 0; i < h; ++i)
                     for (int j = 0; j < h; ++j) {
                         const long double kij = K[(size_t)i * n + j], kim = K[(size_t)i * n + (n - 1 - j)];
-                        At[(size_t)j * h + i] = (double)((kij + kim) / 2.0L);
-                        Bt[(size_t)j * h + i] = (double)((kij - kim) / 2.0L);
+                        Ar[(size_t)i * h + j] = (double)((kij + kim) / 2.0L);
+                        Br[(size_t)i * h + j] = (double)((kij - kim) / 2.0L);
+                    }
+                if (c->psize == 4) {
+                    Ar = round_fp32_colsum(Ar, h, h);
+                    Br = round_fp32_colsum(Br, h, h);
+                }
+                for (int i = 0; i < h; ++i)
+                    for (int j = 0; j < h; ++j) {
+                        At[(size_t)j * h + i] = Ar[(size_t)i * h + j];
+                        Bt[(size_t)j * h + i] = Br[(size_t)i * h + j];
                     }
                 int rc = upload_p(c, &A.kA, At);
                 if (!rc) rc = upload_p(c, &A.kB, Bt);
@@ -526,14 +628,25 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     }
     ALLOC(c->state, sizeof(InstState) * B);
 #undef ALLOC
-    if ((rc = build_axes(c))) {
+    if ((rc = build_axes(c)) || (rc = build_fused2d(c))) {
         scft_ctx_destroy(c);
         return rc;
+    }
+    {
+        /* longest chains first, so the persistent launch ends with short ones */
+        std::vector<int> ord((size_t)B * c->nchains);
+        for (size_t k = 0; k < ord.size(); ++k) ord[k] = (int)k;
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](int x, int y) { return c->chains_h[x].len > c->chains_h[y].len; });
+        if ((rc = upload(c, (void **)&c->order, ord))) {
+            scft_ctx_destroy(c);
+            return rc;
+        }
     }
     c->iter.assign(B, 0);
     c->rng.assign(3 * B, 0);
     c->fields_set.assign(B, 0);
-    c->prop_launches_per_iter = (long)(c->maxlen - 1) * (long)c->axes.size();
+    c->prop_launches_per_iter = c->fused2d ? 1L : (long)(c->maxlen - 1) * (long)c->axes.size();
     c->launches_per_iter = c->prop_launches_per_iter + 2 + 6;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
         set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -628,12 +741,34 @@ static PostArgs post_args(scft_ctx *c, const double *noise_dev)
     a.noise = noise_dev;
     a.hist = c->hist;
     a.hist_cap = c->hist_cap;
+    for (int f = 0; f < SCFT_NFIELDS; ++f) a.part0[f] = a.part1[f] = -1;
+    for (int k = 0; k < c->nblocks; ++k) {
+        const BlockDesc &bd = c->blocks_h[k];
+        if (bd.part == 0)
+            a.part0[bd.field] = k;
+        else
+            a.part1[bd.field] = k;
+    }
     return a;
 }
 
 /* All contour steps of every chain: one launch per axis per step. */
 static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total, int maxlen)
 {
+    if (c->fused2d) {
+        /* one persistent launch: every chain runs its whole contour loop */
+        Step2DArgs a;
+        a.chains = chains;
+        a.order = (chains == c->chains) ? c->order : nullptr;
+        a.s = 0;
+        a.s_end = maxlen - 1;
+        a.sstride = c->sm;
+        a.kz = c->kz_rm;
+        a.twx = c->twx;
+        a.ex = c->ex;
+        CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0));
+        return SCFT_OK;
+    }
     const int npass = (int)c->axes.size();
     for (int s = 0; s < maxlen - 1; ++s) {
         for (int pi = 0; pi < npass; ++pi) {

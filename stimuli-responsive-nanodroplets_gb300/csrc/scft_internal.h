@@ -140,6 +140,11 @@ struct PostArgs {
     const double *noise;        /* [B][n_active][sm] or NULL */
     scft_iter_out *hist;        /* [cap][B] */
     int hist_cap;
+    /* which density blocks make up each field's total (funAddArray operands,
+     * SCFT.c:1486-1495): first operand (diblock or brush block), second
+     * operand (homopolymer block), -1 if absent. Same for every instance. */
+    int part0[SCFT_NFIELDS];
+    int part1[SCFT_NFIELDS];
 };
 
 cudaError_t scft_post_iter_begin(const PostArgs &a, int prec, int sms, cudaStream_t st);
@@ -148,3 +153,20 @@ cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_
 int scft_post_nparts(long m, int sms);
 cudaError_t scft_convert(int prec, const double *src, void *dst, long n, int to_p, cudaStream_t st);
 cudaError_t scft_boltz_one(int prec, const double *w, void *bz, double ds, long m, cudaStream_t st);
+
+/* Arguments of the fused 2D contour step (scft_step2d.cu). */
+struct Step2DArgs {
+    const ChainDesc *chains;
+    const int *order;  /* chain indices, longest first (or NULL) */
+    int s;             /* first contour step: reads slice s */
+    int s_end;         /* runs steps s .. min(s_end, len-1)-1 */
+    long sstride;      /* slice stride (elements) */
+    const void *kz;    /* P[2*H*H]: A[i][k] then B[i][k], H = NZ/2 */
+    const void *twx;   /* Cx<P>[NX]: exp(-2 pi i n2 k1 / NX) at n2*N1 + k1 */
+    const void *ex;    /* P[NX]: E_x(k)/NX */
+};
+
+size_t scft_step2d_smem(int prec, int nx, int nz);
+int scft_step2d_n1(int nx);
+cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
+                               int configure);

@@ -130,27 +130,126 @@ __global__ void k_q_final(PostArgs a, int nparts)
  * reference's index sets (funDensity, SCFT.c:2281-2297): weight 1 at both
  * ends, 4 at odd offsets up to stop-1, 2 at even offsets up to stop-2. For an
  * odd number of intervals the point stop-1 therefore gets no weight, as in
- * the reference. */
+ * the reference. Each thread owns V consecutive points (one 16-byte load per
+ * slice) and the contour loops are unrolled so that several slices are in
+ * flight per thread; products and sums are FP64. */
+/* Contour accumulators. FP64 form: plain FP64. FP32 form: double-float
+ * (hi + lo) sums of exact products (fma gives the rounding error of x*y, Knuth's
+ * TwoSum the error of each addition), which keeps about 48 significant bits,
+ * at FP32 rate; the FP64 pipe of GB300 runs at 1/58 of the FP32 rate and
+ * otherwise bounds this kernel. */
+struct AccD {
+    double s;
+    __device__ __forceinline__ void zero() { s = 0.0; }
+    __device__ __forceinline__ void add(double x, double y) { s += x * y; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+struct AccF {
+    float hi, lo;
+    __device__ __forceinline__ void zero() { hi = lo = 0.0f; }
+    __device__ __forceinline__ void add(float x, float y)
+    {
+        const float p = x * y;
+        const float e = fmaf(x, y, -p);
+        const float t = hi + p;
+        const float bb = t - hi;
+        const float err = (hi - (t - bb)) + (p - bb);
+        hi = t;
+        lo += err + e;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <typename P>
+struct AccOf;
+template <>
+struct AccOf<double> {
+    using T = AccD;
+};
+template <>
+struct AccOf<float> {
+    using T = AccF;
+};
+
+template <typename P, int V>
+__device__ __forceinline__ void load_p(const P *p, P (&o)[V])
+{
+    if (V == 4) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        reinterpret_cast<float *>(o)[0] = t.x;
+        reinterpret_cast<float *>(o)[1] = t.y;
+        reinterpret_cast<float *>(o)[2] = t.z;
+        reinterpret_cast<float *>(o)[3] = t.w;
+    } else {
+        const double2 t = *reinterpret_cast<const double2 *>(p);
+        reinterpret_cast<double *>(o)[0] = t.x;
+        reinterpret_cast<double *>(o)[1] = t.y;
+    }
+}
+
 template <typename P>
 __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
 {
+    constexpr int V = sizeof(P) == 4 ? 4 : 2;
+    using Acc = typename AccOf<P>::T;
     const int blk = blockIdx.y, b = blockIdx.z;
     const BlockDesc bd = a.blocks[blk];
-    const ChainDesc &cf = a.chains[b * a.nchains + bd.chain_f];
-    const ChainDesc &cb = a.chains[b * a.nchains + bd.chain_b];
-    const P *qf = reinterpret_cast<const P *>(cf.q);
-    const P *qb = reinterpret_cast<const P *>(cb.q);
+    const P *qf = reinterpret_cast<const P *>(a.chains[b * a.nchains + bd.chain_f].q);
+    const P *qb = reinterpret_cast<const P *>(a.chains[b * a.nchains + bd.chain_b].q);
     double *out = a.raw + ((long)b * a.nblocks + blk) * a.sm;
     const int top = bd.len - 1;
-    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < a.m; idx += (long)gridDim.x * blockDim.x) {
-        double acc = (double)qf[(long)bd.start * a.sm + idx] * (double)qb[(long)(top - bd.start) * a.sm + idx] +
-                     (double)qf[(long)bd.stop * a.sm + idx] * (double)qb[(long)(top - bd.stop) * a.sm + idx];
-        double a4 = 0.0, a2 = 0.0;
-        for (int s = bd.start + 1; s <= bd.stop - 1; s += 2)
-            a4 += (double)qf[(long)s * a.sm + idx] * (double)qb[(long)(top - s) * a.sm + idx];
-        for (int s = bd.start + 2; s <= bd.stop - 2; s += 2)
-            a2 += (double)qf[(long)s * a.sm + idx] * (double)qb[(long)(top - s) * a.sm + idx];
-        out[idx] = acc + 4.0 * a4 + 2.0 * a2;
+    const long nvec = a.m / V;
+    for (long iv = blockIdx.x * (long)blockDim.x + threadIdx.x; iv < (a.m + V - 1) / V;
+         iv += (long)gridDim.x * blockDim.x) {
+        const long idx = iv * V;
+        if (iv < nvec) {
+            Acc ends[V], a4[V], a2[V];
+            P x[V], y[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                ends[v].zero();
+                a4[v].zero();
+                a2[v].zero();
+            }
+            load_p<P, V>(qf + (long)bd.start * a.sm + idx, x);
+            load_p<P, V>(qb + (long)(top - bd.start) * a.sm + idx, y);
+#pragma unroll
+            for (int v = 0; v < V; ++v) ends[v].add(x[v], y[v]);
+            load_p<P, V>(qf + (long)bd.stop * a.sm + idx, x);
+            load_p<P, V>(qb + (long)(top - bd.stop) * a.sm + idx, y);
+#pragma unroll
+            for (int v = 0; v < V; ++v) ends[v].add(x[v], y[v]);
+#pragma unroll 4
+            for (int s = bd.start + 1; s <= bd.stop - 1; s += 2) {
+                load_p<P, V>(qf + (long)s * a.sm + idx, x);
+                load_p<P, V>(qb + (long)(top - s) * a.sm + idx, y);
+#pragma unroll
+                for (int v = 0; v < V; ++v) a4[v].add(x[v], y[v]);
+            }
+#pragma unroll 4
+            for (int s = bd.start + 2; s <= bd.stop - 2; s += 2) {
+                load_p<P, V>(qf + (long)s * a.sm + idx, x);
+                load_p<P, V>(qb + (long)(top - s) * a.sm + idx, y);
+#pragma unroll
+                for (int v = 0; v < V; ++v) a2[v].add(x[v], y[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v) out[idx + v] = ends[v].value() + 4.0 * a4[v].value() + 2.0 * a2[v].value();
+        } else {
+            for (long i = idx; i < a.m; ++i) {
+                Acc ends, a4, a2;
+                ends.zero();
+                a4.zero();
+                a2.zero();
+                ends.add(qf[(long)bd.start * a.sm + i], qb[(long)(top - bd.start) * a.sm + i]);
+                ends.add(qf[(long)bd.stop * a.sm + i], qb[(long)(top - bd.stop) * a.sm + i]);
+                for (int s = bd.start + 1; s <= bd.stop - 1; s += 2)
+                    a4.add(qf[(long)s * a.sm + i], qb[(long)(top - s) * a.sm + i]);
+                for (int s = bd.start + 2; s <= bd.stop - 2; s += 2)
+                    a2.add(qf[(long)s * a.sm + i], qb[(long)(top - s) * a.sm + i]);
+                out[i] = ends.value() + 4.0 * a4.value() + 2.0 * a2.value();
+            }
+        }
     }
 }
 
@@ -159,11 +258,21 @@ __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
  * funVolFrac SCFT.c:1458-1482), totals (funAddArray SCFT.c:1486-1512), the free
  * energy integrand on pre-update fields (funFreeEnergy SCFT.c:1874-1917), the
  * field update (funUpdate SCFT.c:2044-2117) and the RMS term (SCFT.c:1566-1578).
+ *
+ * Everything runs over the compacted list of active fields: a field that is not
+ * active has no density (its terms in H and in the totals are exact zeros in
+ * the reference) and is not updated. The list, the chi sub-table and the block
+ * factors sit in shared memory; per-point values stay in registers because all
+ * register-array indices are loop counters of fully unrolled loops.
  * Block partials of H, p and (phi_tot-1)^2 go to a.partial. */
 __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
 {
     __shared__ double sh[3 * 32];
     __shared__ double coef[SCFT_MAX_BLOCKS];
+    __shared__ double chiA[SCFT_NFIELDS][SCFT_NFIELDS];
+    __shared__ double pavgA[SCFT_NFIELDS];
+    __shared__ int actf[SCFT_NFIELDS], p0[SCFT_NFIELDS], p1[SCFT_NFIELDS];
+    __shared__ int s_na;
     const int b = blockIdx.y;
     const InstParams &ip = a.params[b];
     const InstState &st = a.state[b];
@@ -171,106 +280,133 @@ __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
     if (threadIdx.x < a.nblocks) {
         const BlockDesc bd = a.blocks[threadIdx.x];
         const double ds_eff = 1.0 / (bd.len - 1);
-        coef[threadIdx.x] = ds_eff / st.q[bd.species];
+        /* frac * ((raw / 3) * (DS_EFF / Q)) as one factor: the FP64 divisions
+         * would otherwise dominate this kernel's FP64 pipe time */
+        coef[threadIdx.x] = ip.frac[threadIdx.x] * ((ds_eff / st.q[bd.species]) / 3.0);
+    }
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int f = 0; f < SCFT_NFIELDS; ++f)
+            if (ip.active[f]) {
+                actf[n] = f;
+                p0[n] = a.part0[f];
+                p1[n] = a.part1[f];
+                pavgA[n] = ip.phi_avg[f];
+                ++n;
+            }
+        s_na = n;
     }
     __syncthreads();
+    const int na = s_na;
+    for (int e = threadIdx.x; e < na * na; e += blockDim.x) {
+        const int i = e / na, j = e - i * na;
+        chiA[i][j] = ip.chi[actf[i]][actf[j]];
+    }
+    __syncthreads();
+    const double g1 = ip.g1, g2 = ip.g2, dt = ip.dt_noise;
+    const double inv_na = 1.0 / na;
+    const int mask = ip.mask;
     double *w = a.w + (long)b * 14 * a.sm;
     double *phi = a.phi + (long)b * 14 * a.sm;
     const double *raw = a.raw + (long)b * a.nblocks * a.sm;
     const double *noise = a.noise ? a.noise + (long)b * ip.n_active * a.sm : nullptr;
-    const bool add_noise = noise && (ip.dt_noise * mf != 0.0);
+    const bool add_noise = noise && (dt * mf != 0.0);
     double acc[3] = {0.0, 0.0, 0.0};
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < a.m; idx += (long)gridDim.x * blockDim.x) {
-        double part[SCFT_NFIELDS][2];
-        int has[SCFT_NFIELDS][2];
-#pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) has[f][0] = has[f][1] = 0;
-        for (int k = 0; k < a.nblocks; ++k) {
-            const BlockDesc bd = a.blocks[k];
-            const double v = ip.frac[k] * ((raw[(long)k * a.sm + idx] / 3.0) * coef[k]);
-            part[bd.field][bd.part] = v;
-            has[bd.field][bd.part] = 1;
-        }
-        double ph[SCFT_NFIELDS];
-#pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) {
-            if (has[f][0] && has[f][1])
-                ph[f] = part[f][0] + part[f][1];
-            else if (has[f][0])
-                ph[f] = part[f][0];
-            else if (has[f][1])
-                ph[f] = part[f][1];
-            else
-                ph[f] = 0.0;
-        }
-        double tot = ph[0] + ph[1];
-#pragma unroll
-        for (int f = 2; f < 10; ++f) tot = tot + ph[f];
-        if (ip.mask) tot = tot + ph[10] + ph[11] + ph[12];
-
-        double wv[SCFT_NFIELDS];
-#pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) wv[f] = w[f * a.sm + idx];
+        double ph[SCFT_NFIELDS], wv[SCFT_NFIELDS], dw[SCFT_NFIELDS];
+        double tot = 0.0, sphi = 0.0, wphi = 0.0, hint = 0.0;
         const double pv = w[13 * a.sm + idx];
-
+        bool first_tot = true;
+#pragma unroll
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
+            const int f = actf[i], b0 = p0[i], b1 = p1[i];
+            /* (raw / 3) * (DS_EFF / Q), then * VOL factor, as funDensity and funVolFrac */
+            double v = 0.0;
+            if (b0 >= 0) v = raw[(long)b0 * a.sm + idx] * coef[b0];
+            if (b1 >= 0) {
+                const double u = raw[(long)b1 * a.sm + idx] * coef[b1];
+                v = (b0 >= 0) ? v + u : u;
+            }
+            ph[i] = v;
+            wv[i] = w[(long)f * a.sm + idx];
+            /* phi_tot adds the free-polymer totals A..J and, with MASK, S1..S3 */
+            if (f < 10 || mask) {
+                tot = first_tot ? v : tot + v;
+                first_tot = false;
+            }
+        }
         /* free-energy integrand on the pre-update fields */
-        double hint = 0.0, sphi = 0.0, wphi = 0.0;
+        bool first_h = true;
 #pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) {
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
 #pragma unroll
-            for (int g = f + 1; g < SCFT_NFIELDS; ++g) hint += ip.chi[f][g] * ph[f] * ph[g];
-            wphi += wv[f] * ph[f];
-            sphi += ph[f];
+            for (int j = i + 1; j < SCFT_NFIELDS; ++j) {
+                if (j >= na) break;
+                const double t = chiA[i][j] * ph[i] * ph[j];
+                hint = first_h ? t : hint + t;
+                first_h = false;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
+            wphi += wv[i] * ph[i];
+            sphi += ph[i];
         }
         hint = hint - wphi - pv * (1.0 - sphi);
-
-        /* field update */
-        double rmr[SCFT_NFIELDS], dw[SCFT_NFIELDS];
+        /* densities out, then reuse ph for phi - phi_avg */
         double rsum = 0.0;
 #pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) {
-            rmr[f] = ip.active[f] ? ph[f] - ip.phi_avg[f] : 0.0;
-            rsum += rmr[f];
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
+            phi[(long)actf[i] * a.sm + idx] = ph[i];
+            ph[i] = ph[i] - pavgA[i];
+            rsum += ph[i];
         }
+        phi[13 * a.sm + idx] = tot;
 #pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) {
-            double d = -wv[f] + pv;
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
+            double d = -wv[i] + pv;
 #pragma unroll
-            for (int g = 0; g < SCFT_NFIELDS; ++g)
-                if (g != f && ip.active[g]) d += ip.chi[f][g] * rmr[g];
-            dw[f] = d;
+            for (int j = 0; j < SCFT_NFIELDS; ++j) {
+                if (j >= na) break;
+                if (j != i) d += chiA[i][j] * ph[j];
+            }
+            dw[i] = d;
         }
-        /* correction: sum over active pairs f<g of chi_fg * sum_{h != f,g} rmr_h
-         * (SCFT.c:2076-2091), written as chi_fg * (R - rmr_f - rmr_g) */
+        /* correction: sum over active pairs f<g of chi_fg * sum_{h != f,g} (phi_h - avg_h)
+         * (SCFT.c:2076-2091), written as chi_fg * (R - r_f - r_g) */
         double corr = 0.0;
-        if (ip.n_active > 1) {
+        if (na > 1) {
 #pragma unroll
-            for (int f = 0; f < SCFT_NFIELDS; ++f) {
-                if (!ip.active[f]) continue;
+            for (int i = 0; i < SCFT_NFIELDS; ++i) {
+                if (i >= na) break;
 #pragma unroll
-                for (int g = f + 1; g < SCFT_NFIELDS; ++g)
-                    if (ip.active[g]) corr += ip.chi[f][g] * (rsum - rmr[f] - rmr[g]);
+                for (int j = i + 1; j < SCFT_NFIELDS; ++j) {
+                    if (j >= na) break;
+                    corr += chiA[i][j] * (rsum - ph[i] - ph[j]);
+                }
             }
         }
         double psum = 0.0;
-        int an = 0;
 #pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) {
-            if (!ip.active[f]) continue;
-            double wn = wv[f];
+        for (int i = 0; i < SCFT_NFIELDS; ++i) {
+            if (i >= na) break;
+            double wn = wv[i];
 #pragma unroll
-            for (int g = 0; g < SCFT_NFIELDS; ++g)
-                if (ip.active[g]) wn += (g == f ? ip.g1 : ip.g2) * dw[g];
-            if (add_noise) wn += ip.dt_noise * mf * noise[(long)an * a.sm + idx];
-            ++an;
-            w[f * a.sm + idx] = wn;
+            for (int j = 0; j < SCFT_NFIELDS; ++j) {
+                if (j >= na) break;
+                wn += (j == i ? g1 : g2) * dw[j];
+            }
+            if (add_noise) wn += dt * mf * noise[(long)i * a.sm + idx];
+            w[(long)actf[i] * a.sm + idx] = wn;
             psum += wn;
         }
-        const double pn = (psum + corr) / ip.n_active;
+        const double pn = (psum + corr) * inv_na;
         w[13 * a.sm + idx] = pn;
-#pragma unroll
-        for (int f = 0; f < SCFT_NFIELDS; ++f) phi[f * a.sm + idx] = ph[f];
-        phi[13 * a.sm + idx] = tot;
         acc[0] += hint;
         acc[1] += pn;
         acc[2] += (tot - 1.0) * (tot - 1.0);
@@ -380,7 +516,8 @@ cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_
     else
         k_q_partial<float><<<gq, POST_THREADS, 0, st>>>(a);
     k_q_final<<<dim3(SCFT_NSPECIES, a.B), 32, 0, st>>>(a, gp);
-    dim3 gd(gp, a.nblocks, a.B);
+    const int vw = prec == SCFT_PREC_FP64 ? 2 : 4;
+    dim3 gd(grid_for((a.m + vw - 1) / vw, sms), a.nblocks, a.B);
     if (prec == SCFT_PREC_FP64)
         k_density<double><<<gd, POST_THREADS, 0, st>>>(a);
     else

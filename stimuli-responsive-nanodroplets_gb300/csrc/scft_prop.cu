@@ -192,6 +192,12 @@ __global__ void __launch_bounds__(256) k_pass_fft(AxisGeom g, PassArgs a)
     for (int e = threadIdx.x; e < nl * n; e += blockDim.x) {
         const int l = e / n, t = e - l * n;
         Cx<P> v = r[l * ldl + t];
+        if (t == 0) {
+            /* mean mode, E(0) = 1: divide by n (correctly rounded) rather than
+             * multiply by a rounded 1/n, so its per-step gain is unbiased */
+            r[l * ldl] = {v.x / (P)n, v.y / (P)n};
+            continue;
+        }
         const P f = spec[t];
         r[l * ldl + t] = {v.x * f, v.y * f};
     }

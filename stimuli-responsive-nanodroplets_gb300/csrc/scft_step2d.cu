@@ -1,0 +1,490 @@
+/*
+ * scft_step2d.cu — one fused launch per contour step for 2D (NY = 1) grids:
+ *   q_{s+1} = b . Kz . Kx . (b . q_s),   b = exp(-DS w / 2)
+ * (funPDESolver_periodic / funPDESolver_DirichletBC, SCFT.c:2474-2631).
+ *
+ * One CTA owns one NX x NZ slice of one chain of one instance, entirely in
+ * shared memory (row pitch NZ+2 keeps the 64/128-bit row accesses of the z
+ * phase conflict-free), so a step reads q_s and b once and writes q_{s+1} once.
+ *
+ *  x axis (periodic): pairs of adjacent z columns form one complex column, as
+ *  the factor is real and even in k. Each complex column of length N = NX =
+ *  N1*N2 is transformed by a four-step FFT with register codelets: A) N2 DFTs
+ *  of length N1 over stride-N2 rows and the twiddle W_N^(n2 k1); B) N1 DFTs of
+ *  length N2 over contiguous row blocks, the factor E(k)/N, the inverse DFTs of
+ *  length N2 and the conjugate twiddle, all in registers; C) the inverse DFTs
+ *  of length N1. Every work item reads and writes the same set of rows, so a
+ *  stage needs no barrier between its loads and stores.
+ *  z axis: y = Kz x with Kz symmetric and centrosymmetric (the DST-I factor of
+ *  the odd extension for MASK 1, the circulant factor for MASK 0) as two
+ *  half-size products on x_k +- x_{NZ-1-k}: each thread keeps its row's
+ *  sums and differences in registers and reads operator rows as broadcast
+ *  128-bit loads (NZ^2/2 multiply-adds per row).
+ */
+#include <cuda_runtime.h>
+
+#include "scft_internal.h"
+
+namespace {
+
+template <typename P>
+struct V2;
+template <>
+struct V2<float> {
+    using T = float2;
+};
+template <>
+struct V2<double> {
+    using T = double2;
+};
+
+template <typename P>
+struct V4;
+template <>
+struct V4<float> {
+    using T = float4; /* 16-byte operator loads */
+    static constexpr int W = 4;
+};
+template <>
+struct V4<double> {
+    using T = double2;
+    static constexpr int W = 2;
+};
+
+template <typename P>
+struct Cx {
+    P x, y;
+};
+
+constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
+
+/* byte offsets of the shared-memory regions: X, KA, KB, TW, EX */
+template <typename P, int NX, int NZ>
+struct Smem2D {
+    static constexpr size_t H = NZ / 2;
+    static constexpr size_t X = 0;
+    static constexpr size_t KA = align16(X + sizeof(P) * NX * (NZ + 2));
+    static constexpr size_t KB = align16(KA + sizeof(P) * H * H);
+    static constexpr size_t TW = align16(KB + sizeof(P) * H * H);
+    static constexpr size_t EX = align16(TW + 2 * sizeof(P) * NX);
+    static constexpr size_t END = align16(EX + sizeof(P) * NX);
+};
+
+template <typename P>
+__device__ __forceinline__ Cx<P> cmul(Cx<P> a, Cx<P> b)
+{
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+/* a * conj(b) */
+template <typename P>
+__device__ __forceinline__ Cx<P> cmulc(Cx<P> a, Cx<P> b)
+{
+    return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+template <typename P>
+__device__ __forceinline__ Cx<P> cadd(Cx<P> a, Cx<P> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename P>
+__device__ __forceinline__ Cx<P> csub(Cx<P> a, Cx<P> b) { return {a.x - b.x, a.y - b.y}; }
+template <typename P, bool INV>
+__device__ __forceinline__ Cx<P> mul_si(Cx<P> a) /* sign*i*a, sign = -1 forward */
+{
+    return INV ? Cx<P>{-a.y, a.x} : Cx<P>{a.y, -a.x};
+}
+
+/* cos and sin of 2 pi k / N for N = 8, 12, 16 */
+__constant__ double c_cos8[8] = {1.0, 0.70710678118654757274, 0.0, -0.70710678118654746172, -1.0,
+                                 -0.70710678118654768376, 0.0, 0.70710678118654735069};
+__constant__ double c_sin8[8] = {0.0, 0.70710678118654746172, 1.0, 0.70710678118654757274, 0.0,
+                                 -0.70710678118654746172, -1.0, -0.70710678118654768376};
+__constant__ double c_cos12[12] = {1.0, 0.86602540378443870761, 0.5, 0.0, -0.5, -0.86602540378443870761,
+                                   -1.0, -0.86602540378443881863, -0.5, 0.0, 0.5, 0.86602540378443837454};
+__constant__ double c_sin12[12] = {0.0, 0.5, 0.86602540378443859659, 1.0, 0.86602540378443870761, 0.5,
+                                   0.0, -0.5, -0.86602540378443837454, -1.0, -0.86602540378443859659, -0.5};
+__constant__ double c_cos16[16] = {1.0, 0.92387953251128673848, 0.70710678118654757274, 0.38268343236508983729,
+                                   0.0, -0.38268343236508972627, -0.70710678118654746172, -0.92387953251128673848,
+                                   -1.0, -0.92387953251128684951, -0.70710678118654768376, -0.38268343236509033689,
+                                   0.0, 0.38268343236509000382, 0.70710678118654735069, 0.92387953251128651644};
+__constant__ double c_sin16[16] = {0.0, 0.38268343236508978178, 0.70710678118654746172, 0.92387953251128673848,
+                                   1.0, 0.92387953251128673848, 0.70710678118654757274, 0.38268343236508989280,
+                                   0.0, -0.38268343236508967076, -0.70710678118654746172, -0.92387953251128651644,
+                                   -1.0, -0.92387953251128662746, -0.70710678118654768376, -0.38268343236509039240};
+
+/* the same tables in FP32 */
+__constant__ float c_cos8f[8] = {1.000000000e+00f, 7.071067812e-01f, 6.123233996e-17f, -7.071067812e-01f, -1.000000000e+00f, -7.071067812e-01f, -1.836970199e-16f, 7.071067812e-01f};
+__constant__ float c_sin8f[8] = {0.000000000e+00f, 7.071067812e-01f, 1.000000000e+00f, 7.071067812e-01f, 1.224646799e-16f, -7.071067812e-01f, -1.000000000e+00f, -7.071067812e-01f};
+__constant__ float c_cos12f[12] = {1.000000000e+00f, 8.660254038e-01f, 5.000000000e-01f, 6.123233996e-17f, -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f, -8.660254038e-01f, -5.000000000e-01f, -1.836970199e-16f, 5.000000000e-01f, 8.660254038e-01f};
+__constant__ float c_sin12f[12] = {0.000000000e+00f, 5.000000000e-01f, 8.660254038e-01f, 1.000000000e+00f, 8.660254038e-01f, 5.000000000e-01f, 1.224646799e-16f, -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f, -8.660254038e-01f, -5.000000000e-01f};
+__constant__ float c_cos16f[16] = {1.000000000e+00f, 9.238795325e-01f, 7.071067812e-01f, 3.826834324e-01f, 6.123233996e-17f, -3.826834324e-01f, -7.071067812e-01f, -9.238795325e-01f, -1.000000000e+00f, -9.238795325e-01f, -7.071067812e-01f, -3.826834324e-01f, -1.836970199e-16f, 3.826834324e-01f, 7.071067812e-01f, 9.238795325e-01f};
+__constant__ float c_sin16f[16] = {0.000000000e+00f, 3.826834324e-01f, 7.071067812e-01f, 9.238795325e-01f, 1.000000000e+00f, 9.238795325e-01f, 7.071067812e-01f, 3.826834324e-01f, 1.224646799e-16f, -3.826834324e-01f, -7.071067812e-01f, -9.238795325e-01f, -1.000000000e+00f, -9.238795325e-01f, -7.071067812e-01f, -3.826834324e-01f};
+
+/* W_N^e = exp(sign 2 pi i e / N) for a compile-time e after unrolling */
+template <typename P, int N, bool INV>
+__device__ __forceinline__ Cx<P> wconst(int e)
+{
+    e %= N;
+    if (sizeof(P) == 4) {
+        const float c = N == 8 ? c_cos8f[e] : (N == 12 ? c_cos12f[e] : c_cos16f[e]);
+        const float s = N == 8 ? c_sin8f[e] : (N == 12 ? c_sin12f[e] : c_sin16f[e]);
+        return {(P)c, INV ? (P)s : (P)-s};
+    }
+    double c, s;
+    if (N == 8) {
+        c = c_cos8[e];
+        s = c_sin8[e];
+    } else if (N == 12) {
+        c = c_cos12[e];
+        s = c_sin12[e];
+    } else {
+        c = c_cos16[e];
+        s = c_sin16[e];
+    }
+    return {(P)c, INV ? (P)s : (P)-s};
+}
+
+/* In-register DFTs, natural order in and out. */
+template <typename P, int N, bool INV>
+struct Dft;
+
+template <typename P, bool INV>
+struct Dft<P, 2, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v)
+    {
+        Cx<P> a = v[0];
+        v[0] = cadd(a, v[1]);
+        v[1] = csub(a, v[1]);
+    }
+};
+
+template <typename P, bool INV>
+struct Dft<P, 3, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v)
+    {
+        const P h = (P)0.86602540378443864676;
+        Cx<P> s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+        Cx<P> c = {v[0].x - (P)0.5 * s.x, v[0].y - (P)0.5 * s.y};
+        Cx<P> e = mul_si<P, INV>(d);
+        v[0] = cadd(v[0], s);
+        v[1] = {c.x + h * e.x, c.y + h * e.y};
+        v[2] = {c.x - h * e.x, c.y - h * e.y};
+    }
+};
+
+template <typename P, bool INV>
+struct Dft<P, 4, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v)
+    {
+        Cx<P> b0 = cadd(v[0], v[2]), b1 = csub(v[0], v[2]);
+        Cx<P> b2 = cadd(v[1], v[3]), b3 = mul_si<P, INV>(csub(v[1], v[3]));
+        v[0] = cadd(b0, b2);
+        v[1] = cadd(b1, b3);
+        v[2] = csub(b0, b2);
+        v[3] = csub(b1, b3);
+    }
+};
+
+/* N = A*B: A-point DFTs over stride-B inputs, twiddles W_N^(b k1), B-point DFTs. */
+template <typename P, int A, int B, bool INV>
+__device__ __forceinline__ void dft_two_factor(Cx<P> *v)
+{
+    constexpr int N = A * B;
+    Cx<P> t[N];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        Cx<P> col[A];
+#pragma unroll
+        for (int a = 0; a < A; ++a) col[a] = v[B * a + b];
+        Dft<P, A, INV>::run(col);
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) t[b * A + k1] = (b * k1 == 0) ? col[k1] : cmul(col[k1], wconst<P, N, INV>(b * k1));
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+        Cx<P> row[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) row[b] = t[b * A + k1];
+        Dft<P, B, INV>::run(row);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = row[k2];
+    }
+}
+
+template <typename P, bool INV>
+struct Dft<P, 8, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v) { dft_two_factor<P, 4, 2, INV>(v); }
+};
+template <typename P, bool INV>
+struct Dft<P, 12, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v) { dft_two_factor<P, 4, 3, INV>(v); }
+};
+template <typename P, bool INV>
+struct Dft<P, 16, INV> {
+    static __device__ __forceinline__ void run(Cx<P> *v) { dft_two_factor<P, 4, 4, INV>(v); }
+};
+
+} // namespace
+
+/* ------------------------------------------------------------------ kernel */
+/* 16-byte asynchronous copy global -> shared (no register staging) */
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem));
+}
+
+/* One CTA runs contour steps s = a.s .. min(a.s_end, len-1)-1 of one chain:
+ * the slice stays in shared memory from step to step (q_{s+1} is written to
+ * HBM for the densities and kept for the next step), the operator tables are
+ * loaded once. Chains are taken longest first through a.order. */
+template <typename P, int NX, int NZ, int N1, int N2>
+__global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
+{
+    static_assert(N1 * N2 == NX, "NX = N1 * N2");
+    static_assert(NZ % 4 == 0, "NZ must be a multiple of 4");
+    constexpr int ZP = NZ + 2;  /* row pitch (elements) */
+    constexpr int ZP2 = ZP / 2; /* row pitch in complex pairs */
+    constexpr int NZ2 = NZ / 2; /* complex columns */
+    constexpr int H = NZ / 2;   /* half size of the z operator */
+    using T2 = typename V2<P>::T;
+
+    const ChainDesc cd = a.chains[a.order ? a.order[blockIdx.x] : blockIdx.x];
+    const int s_end = a.s_end < cd.len - 1 ? a.s_end : cd.len - 1;
+    if (a.s >= s_end) return;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using L = Smem2D<P, NX, NZ>;
+    P *X = reinterpret_cast<P *>(smem_raw + L::X);       /* NX * ZP */
+    P *KA = reinterpret_cast<P *>(smem_raw + L::KA);     /* H * H, row-major [i][k] */
+    P *KB = reinterpret_cast<P *>(smem_raw + L::KB);     /* H * H */
+    Cx<P> *TW = reinterpret_cast<Cx<P> *>(smem_raw + L::TW); /* N: W_N^(n2 k1) at n2*N1 + k1 */
+    P *EX = reinterpret_cast<P *>(smem_raw + L::EX);     /* N: E(k)/N */
+    Cx<P> *XC = reinterpret_cast<Cx<P> *>(X);
+
+    const int tid = threadIdx.x;
+    const P *qs = reinterpret_cast<const P *>(cd.q) + (long)a.s * a.sstride;
+
+    /* operators and tables, once per chain (16-byte asynchronous copies) */
+    {
+        constexpr int VP = 16 / sizeof(P);
+        const P *gA = reinterpret_cast<const P *>(a.kz);
+        for (int e = tid; e < H * H / VP; e += NX) {
+            cp_async16(KA + e * VP, gA + e * VP);
+            cp_async16(KB + e * VP, gA + H * H + e * VP);
+        }
+        const P *gT = reinterpret_cast<const P *>(a.twx);
+        for (int e = tid; e < 2 * NX / VP; e += NX) cp_async16(reinterpret_cast<P *>(TW) + e * VP, gT + e * VP);
+        const P *gE = reinterpret_cast<const P *>(a.ex);
+        for (int e = tid; e < NX / VP; e += NX) cp_async16(EX + e * VP, gE + e * VP);
+    }
+    /* load q_s into the padded rows with asynchronous 2-element copies: every
+     * copy of the slice is in flight at once and none holds a register */
+    for (int e = tid; e < NX * NZ2; e += NX) {
+        const int x = e / NZ2, c = e - x * NZ2;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<T2 *>(X) + x * ZP2 + c);
+        if (sizeof(T2) == 8)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(reinterpret_cast<const T2 *>(qs) + e));
+        else
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(reinterpret_cast<const T2 *>(qs) + e));
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+
+    for (int s = a.s; s < s_end; ++s) {
+    const P *bz = reinterpret_cast<const P *>(s < cd.seg_end ? cd.b0 : cd.b1);
+    P *qn = reinterpret_cast<P *>(cd.q) + (long)(s + 1) * a.sstride;
+    /* A: b . q, DFT_N1 over rows N2*n1 + n2, twiddle, back to rows N2*k1 + n2 */
+    for (int w = tid; w < N2 * NZ2; w += NX) {
+        const int n2 = w / NZ2, c = w - n2 * NZ2;
+        Cx<P> v[N1];
+        T2 bv[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) bv[n1] = reinterpret_cast<const T2 *>(bz)[(N2 * n1 + n2) * NZ2 + c];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) {
+            v[n1] = XC[(N2 * n1 + n2) * ZP2 + c];
+            v[n1].x *= bv[n1].x;
+            v[n1].y *= bv[n1].y;
+        }
+        Dft<P, N1, false>::run(v);
+#pragma unroll
+        for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], TW[n2 * N1 + k1]);
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
+    }
+    __syncthreads();
+    /* B: DFT_N2 over rows N2*k1 .. N2*k1+N2-1, E(k)/N, inverse, conjugate twiddle */
+    for (int w = tid; w < N1 * NZ2; w += NX) {
+        const int k1 = w / NZ2, c = w - k1 * NZ2;
+        Cx<P> u[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) u[n2] = XC[(N2 * k1 + n2) * ZP2 + c];
+        Dft<P, N2, false>::run(u);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            if (k2 == 0 && k1 == 0) {
+                /* mean mode, E(0) = 1: a correctly rounded division by N keeps the
+                 * per-step gain of the mean unbiased (a rounded 1/N would not) */
+                u[0].x = u[0].x / (P)NX;
+                u[0].y = u[0].y / (P)NX;
+                continue;
+            }
+            const P f = EX[k1 + N1 * k2];
+            u[k2].x *= f;
+            u[k2].y *= f;
+        }
+        Dft<P, N2, true>::run(u);
+#pragma unroll
+        for (int n2 = 1; n2 < N2; ++n2) u[n2] = cmulc(u[n2], TW[n2 * N1 + k1]);
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) XC[(N2 * k1 + n2) * ZP2 + c] = u[n2];
+    }
+    __syncthreads();
+    /* C: inverse DFT_N1 back to natural rows */
+    for (int w = tid; w < N2 * NZ2; w += NX) {
+        const int n2 = w / NZ2, c = w - n2 * NZ2;
+        Cx<P> v[N1];
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = XC[(N2 * k1 + n2) * ZP2 + c];
+        Dft<P, N1, true>::run(v);
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) XC[(N2 * n1 + n2) * ZP2 + c] = v[n1];
+    }
+    __syncthreads();
+
+    /* z: one row per thread, y = A (x + Jx) -> s, B (x - Jx) -> d */
+    {
+        P *row = X + tid * ZP;
+        P u[H], v[H];
+#pragma unroll
+        for (int j = 0; j < NZ2; ++j) {
+            const T2 t = reinterpret_cast<const T2 *>(row)[j];
+            /* positions 2j and 2j+1 */
+            if (2 * j < H) {
+                u[2 * j] = t.x;
+                v[2 * j] = t.x;
+            } else {
+                u[NZ - 1 - 2 * j] += t.x;
+                v[NZ - 1 - 2 * j] -= t.x;
+            }
+            if (2 * j + 1 < H) {
+                u[2 * j + 1] = t.y;
+                v[2 * j + 1] = t.y;
+            } else {
+                u[NZ - 2 - 2 * j] += t.y;
+                v[NZ - 2 - 2 * j] -= t.y;
+            }
+        }
+        using T4 = typename V4<P>::T;
+        constexpr int W = V4<P>::W;
+        static_assert(H % W == 0, "operator rows must split into 16-byte loads");
+        /* two output rows per pass: four independent accumulation chains */
+        for (int i = 0; i < H; i += 2) {
+            P s0 = 0, d0 = 0, s1 = 0, d1 = 0;
+            const T4 *ar0 = reinterpret_cast<const T4 *>(KA + i * H);
+            const T4 *br0 = reinterpret_cast<const T4 *>(KB + i * H);
+            const T4 *ar1 = reinterpret_cast<const T4 *>(KA + (i + 1) * H);
+            const T4 *br1 = reinterpret_cast<const T4 *>(KB + (i + 1) * H);
+#pragma unroll
+            for (int k = 0; k < H; k += W) {
+                const T4 a0 = ar0[k / W], b0 = br0[k / W], a1 = ar1[k / W], b1 = br1[k / W];
+                const P *pa0 = reinterpret_cast<const P *>(&a0);
+                const P *pb0 = reinterpret_cast<const P *>(&b0);
+                const P *pa1 = reinterpret_cast<const P *>(&a1);
+                const P *pb1 = reinterpret_cast<const P *>(&b1);
+#pragma unroll
+                for (int r = 0; r < W; ++r) {
+                    s0 += pa0[r] * u[k + r];
+                    d0 += pb0[r] * v[k + r];
+                    s1 += pa1[r] * u[k + r];
+                    d1 += pb1[r] * v[k + r];
+                }
+            }
+            row[i] = s0 + d0;
+            row[NZ - 1 - i] = s0 - d0;
+            row[i + 1] = s1 + d1;
+            row[NZ - 2 - i] = s1 - d1;
+        }
+    }
+    __syncthreads();
+    /* q_{s+1} = b . y: to HBM for the densities, and kept as the next step's input */
+#pragma unroll 4
+    for (int e = tid; e < NX * NZ2; e += NX) {
+        const int x = e / NZ2, c = e - x * NZ2;
+        const T2 y2 = reinterpret_cast<const T2 *>(X)[x * ZP2 + c];
+        const T2 b2 = reinterpret_cast<const T2 *>(bz)[e];
+        T2 o;
+        o.x = y2.x * b2.x;
+        o.y = y2.y * b2.y;
+        reinterpret_cast<T2 *>(qn)[e] = o;
+        reinterpret_cast<T2 *>(X)[x * ZP2 + c] = o;
+    }
+    __syncthreads();
+    } /* contour steps */
+}
+
+/* ---------------------------------------------------------------- dispatch */
+template <typename P, int NX, int NZ, int N1, int N2>
+static size_t smem_bytes_t()
+{
+    return Smem2D<P, NX, NZ>::END;
+}
+
+template <typename P, int NX, int NZ, int N1, int N2>
+static cudaError_t launch_t(const Step2DArgs &a, int nblocks, cudaStream_t st, int configure)
+{
+    const size_t smem = smem_bytes_t<P, NX, NZ, N1, N2>();
+    if (configure)
+        return cudaFuncSetAttribute(k_chain2d<P, NX, NZ, N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem);
+    k_chain2d<P, NX, NZ, N1, N2><<<nblocks, NX, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+#define SCFT_STEP2D_SHAPES(X)                                                                                          \
+    X(192, 96, 16, 12)                                                                                                 \
+    X(192, 128, 16, 12)                                                                                                \
+    X(128, 96, 16, 8)                                                                                                  \
+    X(96, 64, 8, 12)                                                                                                   \
+    X(64, 64, 8, 8)                                                                                                    \
+    X(64, 32, 8, 8)                                                                                                    \
+    X(32, 32, 8, 4)                                                                                                    \
+    X(32, 24, 8, 4)                                                                                                    \
+    X(32, 16, 8, 4)                                                                                                    \
+    X(24, 16, 8, 3)                                                                                                    \
+    X(16, 16, 4, 4)
+
+/* Returns the shared-memory bytes of the fused step for (nx, nz) in this
+ * precision, or 0 if the shape has no fused kernel. Only the FP32 form has
+ * one: an FP64 row pair does not fit in registers, and the FP64 form is bound
+ * by the FP64 units, so it keeps the per-axis passes. */
+size_t scft_step2d_smem(int prec, int nx, int nz)
+{
+#define X(NX_, NZ_, A_, B_)                                                                                           \
+    if (nx == NX_ && nz == NZ_) return prec == SCFT_PREC_FP64 ? 0 : smem_bytes_t<float, NX_, NZ_, A_, B_>();
+    SCFT_STEP2D_SHAPES(X)
+#undef X
+    return 0;
+}
+
+/* configure = 1 raises the kernel's shared-memory limit (call once, outside
+ * any stream capture); configure = 0 launches. */
+cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
+                               int configure)
+{
+#define X(NX_, NZ_, A_, B_)                                                                                           \
+    if (nx == NX_ && nz == NZ_)                                                                                        \
+        return prec == SCFT_PREC_FP64 ? cudaErrorInvalidValue : launch_t<float, NX_, NZ_, A_, B_>(a, nblocks, st, configure);
+    SCFT_STEP2D_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+/* N1 of the four-step factorisation NX = N1 * N2 used for shape nx. */
+int scft_step2d_n1(int nx)
+{
+#define X(NX_, NZ_, A_, B_) \
+    if (nx == NX_) return A_;
+    SCFT_STEP2D_SHAPES(X)
+#undef X
+    return 0;
+}

@@ -94,7 +94,7 @@ class Solver:
     """
 
     def __init__(self, surfaces: Surface | Sequence[Surface], precision: str = "fp64", device: int = 0,
-                 use_graph: bool = False):
+                 use_graph: bool = False, kernel_path: str = "auto"):
         if isinstance(surfaces, Surface):
             surfaces = [surfaces]
         self.surfaces = list(surfaces)
@@ -106,6 +106,7 @@ class Solver:
         opt.device = device
         opt.use_graph = int(bool(use_graph))
         opt.n_instances = self.B
+        opt.kernel_path = {"auto": 0, "passes": 1}[kernel_path]
         self.precision = precision
         h = C.c_void_p()
         L.check(L.lib().scft_ctx_create(arr, C.byref(opt), C.byref(h)), "scft_ctx_create")

@@ -1,0 +1,165 @@
+"""Host side of the library, no GPU: exported symbols, parameter derivation,
+the reference's text formats byte for byte, the drand48 noise replay, readers.
+"""
+import ctypes as C
+import importlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLD, load_golden, surface_from_json
+
+CASES = ["bulk2d", "film2d", "blend3d", "quirks", "seed"]
+
+
+def test_library_exports_every_header_symbol(srn):
+    L = importlib.import_module("stimuli-responsive-nanodroplets_gb300._lib")
+    lib = L.lib()
+    names = L.exported_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_derive_matches_oracle(case, srn, golden, oracle_mod):
+    g = golden(case)
+    S = g["S"]
+    d = srn.derive(S)
+    o = oracle_mod.Oracle(S).derived()
+    assert tuple(d.grid) == o["grid"]
+    assert d.c.n_active == o["n_active"]
+    assert list(d.active) == list(o["active"])
+    lens = list(d.ns_dbk) + list(d.ns_homo) + list(d.ns_s)
+    assert lens == list(o["len"])
+    assert list(d.ns_dbk_x) == list(o["nsx"][:4]) and list(d.ns_dbk_y) == list(o["nsy"][:4])
+    assert d.c.ds == o["ds"]
+    assert [d.c.alphax, d.c.alphay, d.c.alphaz] == list(o["alpha"])
+    assert d.c.coating_vol == o["coating"]
+    assert list(d.phi_avg) == list(o["phi_avg"])
+    assert np.array_equal(d.chi_eff, o["chi"])
+    alphas = list(d.alpha_dbk) + list(d.alpha_homo) + list(d.alpha_s)
+    assert alphas == list(o["alpha_sp"])
+
+
+def test_derive_even_homopolymer_count(srn):
+    """LEN > 1 can leave an even contour count (the '> NS' branch, SCFT.c:173)."""
+    s = srn.Surface(NS=20)
+    s.VOL_HOMO = [1.0] + [0.0] * 9
+    s.LEN_HOMO = [1.55] + [1.0] * 9
+    d = srn.derive(s)
+    assert int(d.ns_homo[0]) == 30
+
+
+def test_volume_check(srn, tmp_path):
+    s = srn.configs.bulk2d(nx=8, nz=8, iters=1)
+    s.VOL_DBK = [0.9, 0.0, 0.0, 0.0]
+    d = srn.derive(s)
+    assert d.status == -5 and not d.c.volume_ok
+    srn.write_volume_error(tmp_path, d.c.volume_sum)
+    want = (GOLD / "text_volfail" / "DENSITY_CHECK_FAIL.error").read_bytes()
+    assert (tmp_path / "DENSITY_CHECK_FAIL.error").read_bytes() == want
+
+
+def test_parameters_h_roundtrip(srn):
+    for s in (srn.configs.film2d(), srn.configs.blend3d(), srn.configs.bulk2d()):
+        t = s.to_parameters_h()
+        s2 = srn.Surface.from_parameters_h(t)
+        assert s2.to_parameters_h() == t
+        assert s2.chi_table() == s.chi_table()
+
+
+def _libc_gauss(state):
+    """Marsaglia polar draws with libc's erand48 (the generator drand48 uses)."""
+    libc = C.CDLL(None)
+    libc.erand48.restype = C.c_double
+    libc.erand48.argtypes = [C.POINTER(C.c_ushort)]
+    while True:
+        x1 = 2.0 * libc.erand48(state) - 1.0
+        x2 = 2.0 * libc.erand48(state) - 1.0
+        w = x1 * x1 + x2 * x2
+        if w < 1.0:
+            break
+    return x1 * np.sqrt((-2.0 * np.log(w)) / w)
+
+
+def test_noise_fill_replays_drand48(srn):
+    s = srn.configs.blend3d(n=4, ns=24, iters=1)
+    d = srn.derive(s)
+    seed = (123, 456, 789)
+    noise, st = srn.noise_fill(seed, d)
+    ref_state = (C.c_ushort * 3)(*seed)
+    nx, ny, nz = d.grid
+    na = d.c.n_active
+    ref = np.empty_like(noise)
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                idx = k + nz * (j + ny * i)
+                for a in range(na):
+                    ref[a, idx] = _libc_gauss(ref_state)
+    assert st == tuple(ref_state)
+    np.testing.assert_allclose(noise, ref, rtol=1e-15, atol=0)
+
+
+def _oracle_run_text(srn, oracle_mod, surface, w0, mask3):
+    """Run the oracle through a text case and write every output with the
+    library's writers, as the reference would at these iterations."""
+    o = oracle_mod.Oracle(surface)
+    o.set_fields(w0)
+    if mask3 is not None:
+        o.set_masks(mask3)
+    o.set_iter(1)
+    o.set_rng((11, 22, 33))
+    return o
+
+
+@pytest.mark.parametrize("name,inputs,mask", [("textcase", "text_inputs", False), ("textfilm", "text_inputs_film", True)])
+def test_writers_byte_exact(name, inputs, mask, srn, oracle_mod, tmp_path):
+    gi = dict(np.load(GOLD / f"{inputs}.npz"))
+    S = surface_from_json(srn, gi["surface"])
+    d = srn.derive(S)
+    m3 = srn.configs.substrate_mask(S) if mask else None
+    o = _oracle_run_text(srn, oracle_mod, S, gi["w0"], m3)
+    saved = (11, 22, 33)
+    for _ in range(int(S.ITER)):
+        r = o.iterate(1)[0]
+        it = int(r[0])
+        rec = srn.IterOut(it, r[1], r[2], r[3], r[4:21], r[21:38], 0)
+        if it % int(S.D_WRT_ENERGIES) == 0:
+            srn.write_energies(tmp_path, d, rec)
+        if it % int(S.D_WRT) == 0 or it == 1:
+            phi, _ = o.densities()
+            srn.write_snapshot(tmp_path, d, it, phi, o.get_fields(), saved)
+            saved = o.get_rng()
+    srn.write_run_params(tmp_path, S, d, 1)
+    ref_dir = GOLD / f"text_{name}"
+    for f in sorted(os.listdir(ref_dir)):
+        got = (tmp_path / f).read_bytes()
+        want = (ref_dir / f).read_bytes()
+        assert got == want, f
+
+
+def test_readers_roundtrip(srn, tmp_path):
+    s = srn.configs.film2d(nx=8, nz=6, ns=16, iters=1)
+    d = srn.derive(s)
+    M = d.M
+    rng = np.random.default_rng(0)
+    w = np.round(rng.uniform(-1, 1, (14, M)), 6)
+    phi = np.round(rng.uniform(0, 1, (13, M)), 6)
+    srn.write_snapshot(tmp_path, d, 7, phi, w, (1, 2, 3))
+    assert srn.read_counter(tmp_path) == 7
+    np.testing.assert_allclose(srn.read_restart_fields(tmp_path, d), w, atol=5e-7)
+    assert srn.read_restart_random(tmp_path) == (1, 2, 3)
+    m = srn.configs.substrate_mask(s)
+    i, j, k = srn.configs.idx_coords(*d.grid)
+    rows = []
+    for kk in range(d.grid[2]):
+        for jj in range(d.grid[1]):
+            for ii in range(d.grid[0]):
+                idx = kk + d.grid[2] * (jj + d.grid[1] * ii)
+                rows.append(f"{m[0, idx]} {m[1, idx]} {m[2, idx]}\n")
+    (tmp_path / "wMask.dat").write_text("".join(rows))
+    np.testing.assert_array_equal(srn.read_mask(tmp_path, d), m)
