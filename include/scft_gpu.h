@@ -166,6 +166,18 @@ int scft_get_densities(scft_ctx *ctx, int instance, double *phi13, double *phi_t
  * steps+1 slices (contour-major, slice 0 = q0). */
 int scft_propagate(scft_ctx *ctx, const double *q0, const double *w, int steps, double *q_out);
 
+/* scft_propagate for callers that must not allocate device memory at run time
+ * (hosts whose memory pools already own the device, code that cannot accept the
+ * device synchronisation cudaMalloc/cudaFree may cause or an allocation failure
+ * mid-run). Same arguments and result; the working buffers live in one fixed
+ * device array of scft_static_scratch_bytes() bytes per GPU, held until exit.
+ * The first call on a device looks up that array's address (make it before any
+ * stream capture). Calls share the array: overlapping calls on one GPU race and
+ * must be serialised by the caller. Sizes that do not fit return SCFT_ERR_PARAM
+ * with a message in scft_last_error(). It has no counterpart in the reference. */
+int scft_propagate_static(scft_ctx *ctx, const double *q0, const double *w, int steps, double *q_out);
+size_t scft_static_scratch_bytes(void);
+
 /* Timing of the last scft_iterate call, measured with CUDA events on the
  * context's stream: total device time, time in propagator-step kernels and
  * the number of propagator-step launches. */

@@ -127,6 +127,8 @@ def lib() -> C.CDLL:
         "scft_get_fields": (I, [VP, I, dp]),
         "scft_get_densities": (I, [VP, I, dp, dp]),
         "scft_propagate": (I, [VP, dp, dp, I, dp]),
+        "scft_propagate_static": (I, [VP, dp, dp, I, dp]),
+        "scft_static_scratch_bytes": (C.c_size_t, []),
         "scft_enable_timing": (I, [VP, I]),
         "scft_get_timing": (I, [VP, P(CTiming)]),
         "scft_last_error": (C.c_char_p, []),

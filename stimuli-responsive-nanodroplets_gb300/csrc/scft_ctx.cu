@@ -1002,3 +1002,22 @@ extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
     *t = c->last_timing;
     return SCFT_OK;
 }
+
+/* ------------------------------------------------- internal hooks */
+/* Used by scft_noalloc.cu: context facts and the contour-step launcher on a
+ * caller-provided chain descriptor. */
+int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st)
+{
+    if (!c) return SCFT_ERR_PARAM;
+    *device = c->device;
+    *prec = c->opt.precision;
+    *m = c->m;
+    *sm = c->sm;
+    *ds = c->der[0].ds;
+    *st = c->stream;
+    return SCFT_OK;
+}
+
+int scft_ctx_run_chain(scft_ctx *c, const ChainDesc *dev_desc, int len) { return launch_steps(c, dev_desc, 1, len); }
+
+void scft_set_error(const char *msg) { set_err("%s", msg); }

@@ -170,3 +170,8 @@ size_t scft_step2d_smem(int prec, int nx, int nz);
 int scft_step2d_n1(int nx);
 cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
                                int configure);
+
+/* Internal hooks of scft_ctx.cu for the allocation-free propagator entry point. */
+int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st);
+int scft_ctx_run_chain(scft_ctx *c, const ChainDesc *dev_desc, int len);
+void scft_set_error(const char *msg);
