@@ -169,36 +169,40 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
         "algorithmic_bytes_per_step": bytes_iter * B,
         "contour_steps_per_instance_iteration": steps_iter,
         "device_bytes": sv.device_bytes,
+        "kernel": (f"k_chain2d<float,{sv.grid[0]},{sv.grid[2]}> (persistent fused contour loop)" if t["fused_chain"]
+                   else "k_pass_fft + k_pass_dense (per-axis passes)"),
     }
     res["achieved_gbs"] = bytes_iter * B / (t["prop_ms"] * 1e-3 / steps) / 1e9
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers: per step the restart
+    # fields of every instance go in, one iteration runs, fields and densities
+    # come back (one strided copy each way for the whole batch)
     if e2e_steps > 0:
+        import ctypes as C
         import torch
         M = sv.M
-        w_host = [torch.empty((14, M), dtype=torch.float64, pin_memory=True).numpy() for _ in range(B)]
-        phi_host = [torch.empty((13, M), dtype=torch.float64, pin_memory=True).numpy() for _ in range(B)]
+        w_host = torch.empty((B, 14, M), dtype=torch.float64, pin_memory=True).numpy()
+        phi_host = torch.empty((B, 14, M), dtype=torch.float64, pin_memory=True).numpy()
         for b in range(B):
-            w_host[b][:] = sv.get_fields(b)
+            w_host[b] = sv.get_fields(b)
         sv.enable_timing(False)
-        import ctypes as C
         Lm = importlib.import_module(f"{PKG}._lib")
         dp = C.POINTER(C.c_double)
         lib = Lm.lib()
         recs = (Lm.CIterOut * B)()
+        wp = w_host.ctypes.data_as(dp)
+        pp = phi_host.ctypes.data_as(dp)
         sync()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            for b in range(B):
-                Lm.check(lib.scft_set_fields(sv._h, b, w_host[b].ctypes.data_as(dp)), "set_fields")
+            Lm.check(lib.scft_set_fields_all(sv._h, wp), "set_fields_all")
             Lm.check(lib.scft_iterate(sv._h, 1, None, recs), "iterate")
-            for b in range(B):
-                Lm.check(lib.scft_get_fields(sv._h, b, w_host[b].ctypes.data_as(dp)), "get_fields")
-                Lm.check(lib.scft_get_densities(sv._h, b, phi_host[b].ctypes.data_as(dp), None), "get_densities")
+            Lm.check(lib.scft_get_fields_all(sv._h, wp), "get_fields_all")
+            Lm.check(lib.scft_get_densities_all(sv._h, pp), "get_densities_all")
         sync()
         e2e = time.perf_counter() - t0
         res["e2e"] = {"value": B * e2e_steps / e2e, "unit": "instance-iterations/s",
                       "h2d_bytes_per_step": B * 14 * M * 8,
-                      "d2h_bytes_per_step": B * (14 + 13) * M * 8 + B * C.sizeof(Lm.CIterOut)}
+                      "d2h_bytes_per_step": B * (14 + 14) * M * 8 + B * C.sizeof(Lm.CIterOut)}
     sv.close()
     return res
 
@@ -359,7 +363,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": f32["achieved_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": f32["achieved_gbs"] / peak, "traffic": traffic,
                      "peak_source": "measured" if PEAKS.exists() else "fallback",
-                     "kernel": "propagator passes (k_pass_fft + k_pass_dense)",
+                     "kernel": f32["kernel"],
                      "algorithmic_bytes_per_launch": f32["algorithmic_bytes_per_step"] / f32["prop_launches_per_step"],
                      "launch_ms": f32["prop_ms_per_step"] / f32["prop_launches_per_step"]},
         "fp64_plain": {"value": world * B / (ms64 * 1e-3), "ms_per_step": ms64, "steps": args.fp64_steps,

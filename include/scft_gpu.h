@@ -160,6 +160,14 @@ int scft_iterate(scft_ctx *ctx, int n, const double *noise, scft_iter_out *out);
 int scft_get_fields(scft_ctx *ctx, int instance, double *w14);
 int scft_get_densities(scft_ctx *ctx, int instance, double *phi13, double *phi_tot);
 
+/* The same transfers for every instance at once (one strided copy each):
+ * w14_all is n_instances consecutive w14 blocks; phi14_all is n_instances
+ * blocks of the 13 total densities followed by phi_tot. Pinned host buffers
+ * make these run at the host link's bandwidth. */
+int scft_set_fields_all(scft_ctx *ctx, const double *w14_all);
+int scft_get_fields_all(scft_ctx *ctx, double *w14_all);
+int scft_get_densities_all(scft_ctx *ctx, double *phi14_all);
+
 /* Unit entry point: contour steps of one block, as funPDESolver does
  * (SCFT.c:2310-2412) in this context's geometry and precision. q0 is the
  * initial slice (M doubles), w the field (M doubles); q_out receives
@@ -186,6 +194,8 @@ typedef struct scft_timing {
     double prop_ms;
     long prop_launches;
     long kernel_launches;
+    int fused_chain;   /* 1: contour steps run in the persistent fused 2D chain kernel */
+    int pad;
 } scft_timing;
 int scft_enable_timing(scft_ctx *ctx, int on);
 int scft_get_timing(const scft_ctx *ctx, scft_timing *t);

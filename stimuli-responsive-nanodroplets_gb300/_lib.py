@@ -94,7 +94,8 @@ class CIterOut(C.Structure):
 
 
 class CTiming(C.Structure):
-    _fields_ = [("total_ms", D), ("prop_ms", D), ("prop_launches", C.c_long), ("kernel_launches", C.c_long)]
+    _fields_ = [("total_ms", D), ("prop_ms", D), ("prop_launches", C.c_long), ("kernel_launches", C.c_long),
+                ("fused_chain", C.c_int), ("pad", C.c_int)]
 
 
 _lib = None
@@ -126,6 +127,9 @@ def lib() -> C.CDLL:
         "scft_iterate": (I, [VP, I, dp, P(CIterOut)]),
         "scft_get_fields": (I, [VP, I, dp]),
         "scft_get_densities": (I, [VP, I, dp, dp]),
+        "scft_set_fields_all": (I, [VP, dp]),
+        "scft_get_fields_all": (I, [VP, dp]),
+        "scft_get_densities_all": (I, [VP, dp]),
         "scft_propagate": (I, [VP, dp, dp, I, dp]),
         "scft_propagate_static": (I, [VP, dp, dp, I, dp]),
         "scft_static_scratch_bytes": (C.c_size_t, []),

@@ -928,6 +928,37 @@ extern "C" int scft_get_densities(scft_ctx *c, int b, double *phi13, double *phi
     return SCFT_OK;
 }
 
+extern "C" int scft_set_fields_all(scft_ctx *c, const double *w14_all)
+{
+    if (!c || !w14_all) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpy2DAsync(c->w, sizeof(double) * c->sm, w14_all, sizeof(double) * c->m, sizeof(double) * c->m,
+                         (size_t)c->B * 14, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int b = 0; b < c->B; ++b) c->fields_set[b] = 1;
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_fields_all(scft_ctx *c, double *w14_all)
+{
+    if (!c || !w14_all) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpy2DAsync(w14_all, sizeof(double) * c->m, c->w, sizeof(double) * c->sm, sizeof(double) * c->m,
+                         (size_t)c->B * 14, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_get_densities_all(scft_ctx *c, double *phi14_all)
+{
+    if (!c || !phi14_all) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpy2DAsync(phi14_all, sizeof(double) * c->m, c->phi, sizeof(double) * c->sm, sizeof(double) * c->m,
+                         (size_t)c->B * 14, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
 extern "C" int scft_propagate(scft_ctx *c, const double *q0, const double *w, int steps, double *q_out)
 {
     if (!c || !q0 || !w || !q_out || steps < 0) return SCFT_ERR_PARAM;
@@ -1000,6 +1031,7 @@ extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
 {
     if (!c || !t) return SCFT_ERR_PARAM;
     *t = c->last_timing;
+    t->fused_chain = c->fused2d;
     return SCFT_OK;
 }
 
