@@ -62,6 +62,8 @@ def workload_surfaces(srn, name: str, batch: int):
             s = srn.configs.bulk2d()
             s.set_chi("A", "B", chi_ab)
             out.append(s)
+        elif name == "blend3d":
+            out.append(srn.configs.blend3d(seed=2 + b))
         else:
             raise SystemExit(f"unknown workload {name}")
     return out
@@ -70,7 +72,14 @@ def workload_surfaces(srn, name: str, batch: int):
 def initial_fields(srn, s, seed):
     if s.MASK:
         return srn.configs.droplet_fields(s, seed=seed), srn.configs.substrate_mask(s)
-    return srn.configs.uniform_fields(s.grid(), seed=seed, amp=0.1), None
+    nf = 9 if s.VOL_DBK[1] > 0 else 2
+    return srn.configs.uniform_fields(s.grid(), seed=seed, amp=0.1, fields=tuple(range(nf))), None
+
+
+def start_iteration(s) -> int:
+    """Restart counter for timed runs: past RELAXATION, so the timed iterations
+    are the noise-free phase (the noise-on phase needs the host draws)."""
+    return max(1, int(s.RELAXATION) + 1) if s.DT_NOISE != 0.0 else 1
 
 
 class ClockSampler:
@@ -145,7 +154,7 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
         sv.set_fields(w, b)
         if m is not None:
             sv.set_masks(m, b)
-        sv.set_iteration(1, b)
+        sv.set_iteration(start_iteration(surfaces[b]), b)
     sv.iterate(warmup)
     sv.enable_timing(True)
     sync()
@@ -329,7 +338,7 @@ def main():
             sv.set_fields(w, b)
             if m is not None:
                 sv.set_masks(m, b)
-            sv.set_iteration(1, b)
+            sv.set_iteration(start_iteration(s), b)
         out = sv.iterate(1)
         torch.cuda.synchronize()
         print(f"profile case: {len(surfaces)} instances, F[0] = {out[0][0].free_energy:.12f}")

@@ -25,6 +25,17 @@
 
 #include "scft_internal.h"
 
+/* Build switches of the fused chain kernel. */
+#ifndef SCFT_FOLD_B
+#define SCFT_FOLD_B 0 /* 1: multiply the next step's b in the store phase (measured slower) */
+#endif
+#ifndef SCFT_F32X2
+#define SCFT_F32X2 1 /* packed f32x2 FMA in the z phase */
+#endif
+#ifndef SCFT_ZROWS
+#define SCFT_ZROWS 2 /* output rows per pass of the packed z phase (2 or 4; measured equal) */
+#endif
+
 namespace {
 
 template <typename P>
@@ -139,6 +150,33 @@ __device__ __forceinline__ Cx<P> wconst(int e)
         s = c_sin16[e];
     }
     return {(P)c, INV ? (P)s : (P)-s};
+}
+
+/* Packed FP32 pairs in one 64-bit register (the f32x2 arithmetic of sm_100+). */
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float lo2(unsigned long long r)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+    return lo;
+}
+__device__ __forceinline__ float hi2(unsigned long long r)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+    return hi;
+}
+/* c + a * b lane-wise, round to nearest */
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
 }
 
 /* In-register DFTs, natural order in and out. */
@@ -289,22 +327,50 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
 
+    /* the first step's input b . q_s; later steps get theirs from the store phase */
+    if (SCFT_FOLD_B) {
+        const P *b_first = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
+#pragma unroll 4
+        for (int e = tid; e < NX * NZ2; e += NX) {
+            const int x = e / NZ2, c = e - x * NZ2;
+            const T2 b2 = reinterpret_cast<const T2 *>(b_first)[e];
+            T2 &v = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
+            v.x *= b2.x;
+            v.y *= b2.y;
+        }
+    }
+    __syncthreads();
+
     for (int s = a.s; s < s_end; ++s) {
     const P *bz = reinterpret_cast<const P *>(s < cd.seg_end ? cd.b0 : cd.b1);
+    const P *bnext = reinterpret_cast<const P *>(s + 1 < cd.seg_end ? cd.b0 : cd.b1);
     P *qn = reinterpret_cast<P *>(cd.q) + (long)(s + 1) * a.sstride;
-    /* A: b . q, DFT_N1 over rows N2*n1 + n2, twiddle, back to rows N2*k1 + n2 */
+    if (!SCFT_FOLD_B) {
+        /* b . q_s in place, b loads issued a batch at a time */
+        constexpr int PER = NZ2;
+        constexpr int BATCH = (PER % 16 == 0) ? 16 : ((PER % 8 == 0) ? 8 : 4);
+        const T2 *b2p = reinterpret_cast<const T2 *>(bz);
+        for (int j0 = 0; j0 < PER; j0 += BATCH) {
+            T2 bb[BATCH];
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) bb[j] = b2p[tid + (j0 + j) * NX];
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) {
+                const int e = tid + (j0 + j) * NX;
+                const int x = e / NZ2, c = e - x * NZ2;
+                T2 &slot = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
+                slot.x *= bb[j].x;
+                slot.y *= bb[j].y;
+            }
+        }
+        __syncthreads();
+    }
+    /* A: DFT_N1 over rows N2*n1 + n2 of b . q_s, twiddle, back to rows N2*k1 + n2 */
     for (int w = tid; w < N2 * NZ2; w += NX) {
         const int n2 = w / NZ2, c = w - n2 * NZ2;
         Cx<P> v[N1];
-        T2 bv[N1];
 #pragma unroll
-        for (int n1 = 0; n1 < N1; ++n1) bv[n1] = reinterpret_cast<const T2 *>(bz)[(N2 * n1 + n2) * NZ2 + c];
-#pragma unroll
-        for (int n1 = 0; n1 < N1; ++n1) {
-            v[n1] = XC[(N2 * n1 + n2) * ZP2 + c];
-            v[n1].x *= bv[n1].x;
-            v[n1].y *= bv[n1].y;
-        }
+        for (int n1 = 0; n1 < N1; ++n1) v[n1] = XC[(N2 * n1 + n2) * ZP2 + c];
         Dft<P, N1, false>::run(v);
 #pragma unroll
         for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], TW[n2 * N1 + k1]);
@@ -377,6 +443,44 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         using T4 = typename V4<P>::T;
         constexpr int W = V4<P>::W;
         static_assert(H % W == 0, "operator rows must split into 16-byte loads");
+        if constexpr (sizeof(P) == 4 && SCFT_F32X2) {
+            /* packed FP32 pairs: each f32x2 FMA adds an (even k, odd k) pair of one
+             * output row, so one 128-bit operator load feeds two packed FMAs */
+            unsigned long long u2[H / 2], v2[H / 2];
+#pragma unroll
+            for (int j = 0; j < H / 2; ++j) {
+                u2[j] = pack2(u[2 * j], u[2 * j + 1]);
+                v2[j] = pack2(v[2 * j], v[2 * j + 1]);
+            }
+            constexpr int R = (SCFT_ZROWS == 4 && H % 4 == 0) ? 4 : 2;
+            for (int i = 0; i < H; i += R) {
+                unsigned long long sacc[R], dacc[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) sacc[r] = dacc[r] = 0ull;
+#pragma unroll
+                for (int k = 0; k < H; k += 4) {
+                    float4 av[R], bv[R];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        av[r] = reinterpret_cast<const float4 *>(KA + (i + r) * H)[k / 4];
+                        bv[r] = reinterpret_cast<const float4 *>(KB + (i + r) * H)[k / 4];
+                    }
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        sacc[r] = fma2(pack2(av[r].x, av[r].y), u2[k / 2], sacc[r]);
+                        sacc[r] = fma2(pack2(av[r].z, av[r].w), u2[k / 2 + 1], sacc[r]);
+                        dacc[r] = fma2(pack2(bv[r].x, bv[r].y), v2[k / 2], dacc[r]);
+                        dacc[r] = fma2(pack2(bv[r].z, bv[r].w), v2[k / 2 + 1], dacc[r]);
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const float sr = lo2(sacc[r]) + hi2(sacc[r]), dr = lo2(dacc[r]) + hi2(dacc[r]);
+                    row[i + r] = sr + dr;
+                    row[NZ - 1 - i - r] = sr - dr;
+                }
+            }
+        } else
         /* two output rows per pass: four independent accumulation chains */
         for (int i = 0; i < H; i += 2) {
             P s0 = 0, d0 = 0, s1 = 0, d1 = 0;
@@ -406,17 +510,38 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         }
     }
     __syncthreads();
-    /* q_{s+1} = b . y: to HBM for the densities, and kept as the next step's input */
-#pragma unroll 4
-    for (int e = tid; e < NX * NZ2; e += NX) {
-        const int x = e / NZ2, c = e - x * NZ2;
-        const T2 y2 = reinterpret_cast<const T2 *>(X)[x * ZP2 + c];
-        const T2 b2 = reinterpret_cast<const T2 *>(bz)[e];
-        T2 o;
-        o.x = y2.x * b2.x;
-        o.y = y2.y * b2.y;
-        reinterpret_cast<T2 *>(qn)[e] = o;
-        reinterpret_cast<T2 *>(X)[x * ZP2 + c] = o;
+    /* q_{s+1} = b . y to HBM for the densities. With SCFT_FOLD_B the next step's
+     * input b_next . q_{s+1} stays in shared memory (b_next differs from b only
+     * at the diblock junction); otherwise q_{s+1} does and the next step
+     * multiplies by its b first. Each thread issues a whole batch of b loads
+     * before using any, so L2 latency is paid once per batch. */
+    {
+        constexpr int PER = NZ2; /* pairs per thread */
+        constexpr int BATCH = (PER % 16 == 0) ? 16 : ((PER % 8 == 0) ? 8 : 4);
+        const T2 *b2p = reinterpret_cast<const T2 *>(bz);
+        const T2 *n2p = reinterpret_cast<const T2 *>(bnext);
+        const bool same_b = (bnext == bz);
+        for (int j0 = 0; j0 < PER; j0 += BATCH) {
+            T2 bb[BATCH];
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) bb[j] = b2p[tid + (j0 + j) * NX];
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) {
+                const int e = tid + (j0 + j) * NX;
+                const int x = e / NZ2, c = e - x * NZ2;
+                T2 &slot = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
+                T2 o = slot;
+                o.x *= bb[j].x;
+                o.y *= bb[j].y;
+                reinterpret_cast<T2 *>(qn)[e] = o;
+                if (SCFT_FOLD_B) {
+                    const T2 nb = same_b ? bb[j] : n2p[e];
+                    o.x *= nb.x;
+                    o.y *= nb.y;
+                }
+                slot = o;
+            }
+        }
     }
     __syncthreads();
     } /* contour steps */
