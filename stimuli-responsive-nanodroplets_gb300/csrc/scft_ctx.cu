@@ -71,6 +71,11 @@ struct scft_ctx {
     int fused2d = 0;
     void *kz_rm = nullptr, *twx = nullptr, *ex = nullptr;
     int *order = nullptr; /* chain indices, longest first */
+    /* device noise replay (SCFT_NOISE_DRAND48) */
+    unsigned long long *rng_in = nullptr;
+    int *rng_counts = nullptr;
+    long *rng_prefix = nullptr, *rng_total = nullptr;
+    long rng_chunks = 0;
     /* device memory */
     double *w = nullptr, *phi = nullptr, *raw = nullptr, *mask = nullptr, *partial = nullptr, *noise = nullptr;
     void *bz = nullptr;
@@ -469,8 +474,8 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         scft_options_default(&opt);
     if (opt.n_instances < 1) opt.n_instances = 1;
     if (opt.precision != SCFT_PREC_FP64 && opt.precision != SCFT_PREC_FP32) return SCFT_ERR_PARAM;
-    if (opt.noise_mode != SCFT_NOISE_HOST) {
-        set_err("noise_mode %d is not available in this build", opt.noise_mode);
+    if (opt.noise_mode != SCFT_NOISE_HOST && opt.noise_mode != SCFT_NOISE_DRAND48) {
+        set_err("unknown noise_mode %d", opt.noise_mode);
         return SCFT_ERR_PARAM;
     }
     int ndev = 0;
@@ -627,6 +632,18 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         return rc;
     }
     ALLOC(c->state, sizeof(InstState) * B);
+    if (opt.noise_mode == SCFT_NOISE_DRAND48) {
+        c->rng_chunks = scft_noise_chunks(c->m, d.n_active);
+        ALLOC(c->rng_in, sizeof(unsigned long long) * B);
+        ALLOC(c->rng_counts, sizeof(int) * B * c->rng_chunks);
+        ALLOC(c->rng_prefix, sizeof(long) * B * c->rng_chunks);
+        ALLOC(c->rng_total, sizeof(long) * B);
+        if (scft_noise_setup() != cudaSuccess) {
+            set_err("noise set-up failed");
+            scft_ctx_destroy(c);
+            return SCFT_ERR_CUDA;
+        }
+    }
 #undef ALLOC
     if ((rc = build_axes(c)) || (rc = build_fused2d(c))) {
         scft_ctx_destroy(c);
@@ -647,7 +664,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     c->rng.assign(3 * B, 0);
     c->fields_set.assign(B, 0);
     c->prop_launches_per_iter = c->fused2d ? 1L : (long)(c->maxlen - 1) * (long)c->axes.size();
-    c->launches_per_iter = c->prop_launches_per_iter + 2 + 6;
+    c->launches_per_iter = c->prop_launches_per_iter + 2 + 6 + (opt.noise_mode == SCFT_NOISE_DRAND48 ? 5 : 0);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
         set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
         scft_ctx_destroy(c);
@@ -703,12 +720,28 @@ extern "C" int scft_set_rng(scft_ctx *c, int b, const unsigned short seed[3])
 {
     if (!c || !seed || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
     memcpy(&c->rng[3 * b], seed, 3 * sizeof(unsigned short));
+    if (c->opt.noise_mode == SCFT_NOISE_DRAND48) {
+        cudaSetDevice(c->device);
+        const unsigned long long x = ((unsigned long long)seed[2] << 32) | ((unsigned long long)seed[1] << 16) | seed[0];
+        CK(cudaMemcpyAsync(&c->state[b].rng, &x, sizeof(x), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
     return SCFT_OK;
 }
 
 extern "C" int scft_get_rng(const scft_ctx *c, int b, unsigned short seed[3])
 {
     if (!c || !seed || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    if (c->opt.noise_mode == SCFT_NOISE_DRAND48) {
+        cudaSetDevice(c->device);
+        unsigned long long x = 0;
+        CK(cudaMemcpyAsync(&x, &c->state[b].rng, sizeof(x), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        seed[0] = (unsigned short)(x & 0xFFFF);
+        seed[1] = (unsigned short)((x >> 16) & 0xFFFF);
+        seed[2] = (unsigned short)((x >> 32) & 0xFFFF);
+        return SCFT_OK;
+    }
     memcpy(seed, &c->rng[3 * b], 3 * sizeof(unsigned short));
     return SCFT_OK;
 }
@@ -799,6 +832,24 @@ static int launch_iteration(scft_ctx *c, const double *noise_dev, int slot)
     PostArgs a = post_args(c, noise_dev);
     if (c->timing) CK(cudaEventRecord(c->ev[2 + 2 * slot], c->stream));
     CK(scft_post_iter_begin(a, c->opt.precision, c->sms, c->stream));
+    if (c->opt.noise_mode == SCFT_NOISE_DRAND48) {
+        NoiseArgs na;
+        na.state = c->state;
+        na.params = c->params;
+        na.state_in = c->rng_in;
+        na.counts = c->rng_counts;
+        na.prefix = c->rng_prefix;
+        na.total = c->rng_total;
+        na.noise = c->noise;
+        na.nchunks = c->rng_chunks;
+        na.m = c->m;
+        na.sm = c->sm;
+        na.nx = c->nx;
+        na.ny = c->ny;
+        na.nz = c->nz;
+        na.B = c->B;
+        CK(scft_noise_launch(na, c->stream));
+    }
     int rc = launch_steps(c, c->chains, c->B * c->nchains, c->maxlen);
     if (rc) return rc;
     if (c->timing) CK(cudaEventRecord(c->ev[3 + 2 * slot], c->stream));
@@ -815,7 +866,11 @@ extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_o
             return SCFT_ERR_STATE;
         }
     cudaSetDevice(c->device);
-    if (!noise) {
+    if (noise && c->opt.noise_mode == SCFT_NOISE_DRAND48) {
+        set_err("this context draws its noise on the device; pass NULL");
+        return SCFT_ERR_PARAM;
+    }
+    if (!noise && c->opt.noise_mode == SCFT_NOISE_HOST) {
         /* without noise arrays every iteration must have MF*DT_NOISE == 0 */
         for (int b = 0; b < c->B; ++b)
             for (int k = 1; k <= n; ++k) {
@@ -864,7 +919,7 @@ extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_o
                 }
                 CK(cudaGraphLaunch(c->graph_exec, c->stream));
             } else {
-                int rc = launch_iteration(c, nd, k);
+                int rc = launch_iteration(c, c->opt.noise_mode == SCFT_NOISE_DRAND48 ? c->noise : nd, k);
                 if (rc) return rc;
             }
         }

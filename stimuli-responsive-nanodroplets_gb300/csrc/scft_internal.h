@@ -80,6 +80,7 @@ struct InstParams {
 struct InstState {
     unsigned long iter;   /* iIter, incremented at the start of each iteration */
     unsigned long iter0;  /* value at the start of the current scft_iterate call */
+    unsigned long long rng; /* 48-bit drand48 state (device noise replay) */
     double q[SCFT_NSPECIES];
     double p_avg;
     int status;
@@ -175,3 +176,22 @@ cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, in
 int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st);
 int scft_ctx_run_chain(scft_ctx *c, const ChainDesc *dev_desc, int len);
 void scft_set_error(const char *msg);
+
+/* Device replay of the drand48 noise stream (scft_noise.cu). */
+struct NoiseArgs {
+    InstState *state;
+    const InstParams *params;
+    unsigned long long *state_in; /* [B] state at the start of the iteration */
+    int *counts;                  /* [B][nchunks] */
+    long *prefix;                 /* [B][nchunks] */
+    long *total;                  /* [B] */
+    double *noise;                /* [B][n_active][sm] */
+    long nchunks;
+    long m, sm;
+    int nx, ny, nz;
+    int B;
+};
+
+long scft_noise_chunks(long m, int n_active);
+cudaError_t scft_noise_setup(void);
+cudaError_t scft_noise_launch(const NoiseArgs &n, cudaStream_t st);

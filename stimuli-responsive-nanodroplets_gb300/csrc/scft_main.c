@@ -12,7 +12,8 @@
  * cadence. The hot path runs on the GPU through the C ABI of scft_gpu.h.
  *
  * The FP64 plain form is the default; SCFT_GB300_PRECISION=fp32 selects the
- * FP32-propagator form. The file-name macros of parameters.h are not read: the
+ * FP32-propagator form. The drand48 noise stream is replayed on the device;
+ * SCFT_GB300_NOISE=host draws it on the host instead (same numbers). The file-name macros of parameters.h are not read: the
  * files carry the reference's default names.
  */
 #include <math.h>
@@ -147,32 +148,52 @@ int main(void)
     scft_options_default(&opt);
     const char *prec = getenv("SCFT_GB300_PRECISION");
     if (prec && strcmp(prec, "fp32") == 0) opt.precision = SCFT_PREC_FP32;
+    const char *nm = getenv("SCFT_GB300_NOISE");
+    const int host_noise = nm && strcmp(nm, "host") == 0;
+    opt.noise_mode = host_noise ? SCFT_NOISE_HOST : SCFT_NOISE_DRAND48;
     scft_ctx *ctx = NULL;
     check(scft_ctx_create(&S, &opt, &ctx), "scft_ctx_create");
     check(scft_set_fields(ctx, 0, w14), "scft_set_fields");
     if (S.mask) check(scft_set_masks(ctx, 0, mask3), "scft_set_masks");
     check(scft_set_iteration(ctx, 0, iter), "scft_set_iteration");
+    if (!host_noise) check(scft_set_rng(ctx, 0, seed), "scft_set_rng");
 
     /* restart_random.dat carries the state saved at the previous snapshot, as
      * the reference's seed48 sequence leaves it (SCFT.c:1653-1662) */
     unsigned short saved[3] = {seed[0], seed[1], seed[2]};
-    while (iter <= (unsigned long)S.iter) { /* SCFT.c:1088 */
-        const unsigned long it = iter + 1;
-        const double mf = it > (unsigned long)S.relaxation ? 0.0 : 1.0;
-        const int need = mf * S.dt_noise != 0.0;
-        /* the reference draws its noise every iteration, used or not */
-        scft_noise_fill(seed, &d, need ? noise : NULL);
-        scft_iter_out rec;
-        check(scft_iterate(ctx, 1, need ? noise : NULL, &rec), "scft_iterate");
-        iter = it;
-        if (fmod((double)it, (double)S.d_wrt_energies) == 0) check(scft_write_energies(NULL, &d, &rec), "energies");
-        if (fmod((double)it, (double)S.d_wrt) == 0 || it == 1) {
+    enum { CHUNK = 256 };
+    scft_iter_out *recs = malloc(sizeof(scft_iter_out) * CHUNK);
+    if (!recs) die("Error allocating host buffers");
+    while (iter <= (unsigned long)S.iter) { /* SCFT.c:1088: iterations iter+1 .. ITER+1 */
+        /* run up to the next snapshot (or CHUNK iterations) in one call */
+        unsigned long last = iter + 1;
+        while (last < (unsigned long)S.iter + 1 && last - iter < CHUNK && !(fmod((double)last, (double)S.d_wrt) == 0 || last == 1))
+            ++last;
+        int n = (int)(last - iter);
+        if (host_noise) n = 1;
+        for (int k = 0; k < n && host_noise; ++k) {
+            const unsigned long it = iter + 1;
+            const double mf = it > (unsigned long)S.relaxation ? 0.0 : 1.0;
+            const int need = mf * S.dt_noise != 0.0;
+            /* the reference draws its noise every iteration, used or not */
+            scft_noise_fill(seed, &d, need ? noise : NULL);
+            check(scft_iterate(ctx, 1, need ? noise : NULL, recs), "scft_iterate");
+        }
+        if (!host_noise) check(scft_iterate(ctx, n, NULL, recs), "scft_iterate");
+        for (int k = 0; k < n; ++k) {
+            const unsigned long it = iter + 1 + (unsigned long)k;
+            if (fmod((double)it, (double)S.d_wrt_energies) == 0) check(scft_write_energies(NULL, &d, &recs[k]), "energies");
+        }
+        iter += (unsigned long)n;
+        if (fmod((double)iter, (double)S.d_wrt) == 0 || iter == 1) {
+            if (!host_noise) check(scft_get_rng(ctx, 0, seed), "scft_get_rng");
             check(scft_get_fields(ctx, 0, w14), "scft_get_fields");
             check(scft_get_densities(ctx, 0, phi13, NULL), "scft_get_densities");
-            check(scft_write_snapshot(NULL, &d, it, phi13, w14, saved), "snapshot");
+            check(scft_write_snapshot(NULL, &d, iter, phi13, w14, saved), "snapshot");
             memcpy(saved, seed, sizeof(saved));
         }
     }
+    free(recs);
     scft_ctx_destroy(ctx);
     free(mask3);
     free(w14);

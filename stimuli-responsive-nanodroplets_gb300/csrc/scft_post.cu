@@ -458,7 +458,7 @@ __global__ void k_finalize(PostArgs a, int nparts)
     const double rms = sqrt(v[2] / dvol);
     if (!isfinite(H) || !isfinite(rms) || !isfinite(pavg)) bad = 1;
     st.p_avg = pavg;
-    st.status = bad ? SCFT_ERR_NONFINITE : SCFT_OK;
+    if (bad) st.status = SCFT_ERR_NONFINITE; /* keeps an error set earlier in the iteration */
     rec.iter = st.iter;
     rec.free_energy = H;
     rec.rms = rms;

@@ -25,9 +25,10 @@ from .surface import Surface
 class Run:
     def __init__(self, surface: Surface, w14: Optional[np.ndarray] = None, counter: int = 1, seed=(0, 0, 0),
                  mask3: Optional[np.ndarray] = None, precision: str = "fp64", outdir=None, use_graph: bool = False,
-                 solver: Optional[S.Solver] = None):
+                 solver: Optional[S.Solver] = None, noise: str = "host"):
         self.surface = surface
-        self.solver = solver or S.Solver(surface, precision=precision, use_graph=use_graph)
+        self.solver = solver or S.Solver(surface, precision=precision, use_graph=use_graph, noise=noise)
+        self.device_noise = self.solver.noise_mode == "device"
         self.d = self.solver.derived[0]
         M = self.solver.M
         if counter == 0:
@@ -42,6 +43,8 @@ class Run:
         self.solver.set_iteration(counter)
         self.iter = int(counter)
         self.rng = tuple(int(x) for x in seed)
+        if self.device_noise:
+            self.solver.set_rng(self.rng)
         self.rng_saved = self.rng
         self.outdir = Path(outdir) if outdir is not None else None
         self.records: List[S.IterOut] = []
@@ -61,17 +64,22 @@ class Run:
         s = self.surface
         for _ in range(n):
             it = self.iter + 1
-            t0 = time.perf_counter()
-            need = self._mf(it) * s.DT_NOISE != 0.0
-            noise, self.rng = S.noise_fill(self.rng, self.d, out=need)
-            self.noise_ms += (time.perf_counter() - t0) * 1e3
-            rec = self.solver.iterate(1, noise[None] if need else None)[0][0]
+            if self.device_noise:
+                rec = self.solver.iterate(1)[0][0]
+            else:
+                t0 = time.perf_counter()
+                need = self._mf(it) * s.DT_NOISE != 0.0
+                noise, self.rng = S.noise_fill(self.rng, self.d, out=need)
+                self.noise_ms += (time.perf_counter() - t0) * 1e3
+                rec = self.solver.iterate(1, noise[None] if need else None)[0][0]
             self.iter = it
             out.append(rec)
             self.records.append(rec)
             if self.outdir is not None and it % int(s.D_WRT_ENERGIES) == 0:
                 S.write_energies(self.outdir, self.d, rec)
             if it % int(s.D_WRT) == 0 or it == 1:
+                if self.device_noise:
+                    self.rng = self.solver.get_rng()
                 written = self.rng_saved
                 self.rng_saved = self.rng
                 if self.outdir is not None or keep_snapshots:

@@ -91,10 +91,12 @@ class Solver:
 
     precision: "fp64" (plain form, the drop-in) or "fp32" (FP32 propagators,
     FP64 densities/Q/free energy/update).
+    noise: "host" (the caller passes the drand48 draws to iterate) or "device"
+    (the library replays the drand48 stream itself from set_rng's state).
     """
 
     def __init__(self, surfaces: Surface | Sequence[Surface], precision: str = "fp64", device: int = 0,
-                 use_graph: bool = False, kernel_path: str = "auto"):
+                 use_graph: bool = False, kernel_path: str = "auto", noise: str = "host"):
         if isinstance(surfaces, Surface):
             surfaces = [surfaces]
         self.surfaces = list(surfaces)
@@ -107,6 +109,8 @@ class Solver:
         opt.use_graph = int(bool(use_graph))
         opt.n_instances = self.B
         opt.kernel_path = {"auto": 0, "passes": 1}[kernel_path]
+        opt.noise_mode = {"host": L.NOISE_HOST, "device": L.NOISE_DRAND48}[noise]
+        self.noise_mode = noise
         self.precision = precision
         h = C.c_void_p()
         L.check(L.lib().scft_ctx_create(arr, C.byref(opt), C.byref(h)), "scft_ctx_create")
