@@ -113,9 +113,11 @@ typedef struct scft_options {
 
 void scft_options_default(scft_options *o);
 
-/* Create a context for n_instances solves that share grid and contour counts
- * (surfaces[b] may differ in chi, G1, DT_NOISE, ...). Allocates all device
- * memory up front (fields, propagators, densities).
+/* Create a context for n_instances solves that share the grid, MASK and the
+ * set of species present (surfaces[b] may differ in NS, LEN_*, F_INPUT_*, box
+ * lengths, chi, G1, DT_NOISE, ...). Allocates all device memory up front
+ * (fields, propagators, densities). Instances whose diffusion factors agree
+ * share one set of operator tables.
  * Replaces: allocation and plan setup SCFT.c:433-701 and aExpArg SCFT.c:983-1023. */
 int scft_ctx_create(const scft_surface *surfaces, const scft_options *opt, scft_ctx **out);
 int scft_ctx_destroy(scft_ctx *ctx);
@@ -128,8 +130,26 @@ int scft_set_fields(scft_ctx *ctx, int instance, const double *w14);
 /* Upload the three grafting masks (S1, S2, S3; 3*M doubles).
  * Replaces: wMask.dat read SCFT.c:756-781. */
 int scft_set_masks(scft_ctx *ctx, int instance, const double *mask3);
-/* Set the iteration counter (the value read from counter.dat, SCFT.c:704-716). */
+/* Set the iteration counter (the value read from counter.dat, SCFT.c:704-716).
+ * Also re-arms an instance that a stop criterion froze. */
 int scft_set_iteration(scft_ctx *ctx, int instance, unsigned long iter);
+/* Convergence-driven stopping (no counterpart in the reference, which always
+ * runs ITER iterations; SCFT.c:1088): once an iteration ends with
+ * RMS(phi_tot - 1) < rms_tol the instance is frozen. Later iterations of the
+ * context skip all of its work (contour steps, densities, update, noise draws),
+ * and its records repeat the converging iteration with converged = 1.
+ * rms_tol = 0 (the default) keeps the fixed-ITER semantics. */
+int scft_set_stop(scft_ctx *ctx, int instance, double rms_tol);
+/* Freeze an instance now (an idle slot): later iterations skip it until
+ * scft_set_iteration re-arms it. */
+int scft_freeze(scft_ctx *ctx, int instance);
+/* Give slot `instance` a new surface (continuous batching: a finished solve's
+ * slot takes the next request). The surface must match the context's grid,
+ * MASK, active fields and species composition, and every chain must fit the
+ * contour slices allocated for the slot at creation (create the context with
+ * the largest NS the slot will serve). New diffusion factors add an operator
+ * set. Follow with scft_set_fields / scft_set_iteration. */
+int scft_set_surface(scft_ctx *ctx, int instance, const scft_surface *s);
 /* Set the 48-bit drand48 state (restart_random.dat, SCFT.c:867-878). */
 int scft_set_rng(scft_ctx *ctx, int instance, const unsigned short seed[3]);
 int scft_get_rng(const scft_ctx *ctx, int instance, unsigned short seed[3]);
@@ -143,7 +163,7 @@ typedef struct scft_iter_out {
     double mu[SCFT_NSPECIES];    /* chemPot_* = -ln(Q^2)/2 (SCFT.c:1837-1872) */
     double q[SCFT_NSPECIES];     /* Qsum_* */
     int status;                  /* SCFT_OK or SCFT_ERR_NONFINITE */
-    int pad;
+    int converged;               /* 1: the stop criterion of scft_set_stop has been met */
 } scft_iter_out;
 
 /* Run n SCFT iterations on every instance (one pass of SCFT.c:1088-1580 each).
@@ -154,6 +174,48 @@ typedef struct scft_iter_out {
  * out: NULL or n * n_instances records, [iteration][instance].
  * Replaces: the loop body SCFT.c:1090-1580. */
 int scft_iterate(scft_ctx *ctx, int n, const double *noise, scft_iter_out *out);
+
+/* scft_iterate in two halves, so that the host can keep several contexts (on
+ * their own streams) busy at once: _async enqueues n <= SCFT_HIST_CAP
+ * iterations without waiting (no host noise: SCFT_NOISE_DRAND48 or
+ * MF*DT_NOISE == 0 throughout); _wait blocks until they finish and copies the
+ * n * n_instances records to out (may be NULL). */
+#define SCFT_HIST_CAP 256
+int scft_iterate_async(scft_ctx *ctx, int n);
+int scft_iterate_wait(scft_ctx *ctx, scft_iter_out *out);
+
+/* Batching form over uneven grid sizes (no counterpart in the reference, which
+ * runs one instance per process). A batch groups n surfaces by grid, MASK,
+ * active fields and species composition into one context per group (own
+ * stream, persistent chain kernel over the group's chains, optional CUDA graph
+ * from opt->use_graph) and runs the groups side by side. Instance i is
+ * addressed by its index in surfaces[]; scft_batch_locate gives its context
+ * and slot for the per-context calls. */
+typedef struct scft_batch scft_batch;
+typedef struct scft_batch_result {
+    unsigned long iterations; /* iterations run by the last scft_batch_run */
+    unsigned long iter;       /* iIter after it */
+    double free_energy;       /* of the last iteration run */
+    double rms;
+    int converged;            /* the stop criterion (scft_batch_set_stop) was met */
+    int status;
+} scft_batch_result;
+int scft_batch_create(const scft_surface *surfaces, int n, const scft_options *opt, scft_batch **out);
+int scft_batch_destroy(scft_batch *b);
+int scft_batch_groups(const scft_batch *b);
+int scft_batch_locate(const scft_batch *b, int instance, int *group, int *slot);
+scft_ctx *scft_batch_context(scft_batch *b, int group);
+int scft_batch_set_fields(scft_batch *b, int instance, const double *w14);
+int scft_batch_set_masks(scft_batch *b, int instance, const double *mask3);
+int scft_batch_set_iteration(scft_batch *b, int instance, unsigned long iter);
+int scft_batch_set_rng(scft_batch *b, int instance, const unsigned short seed[3]);
+int scft_batch_set_stop(scft_batch *b, int instance, double rms_tol);
+int scft_batch_get_fields(scft_batch *b, int instance, double *w14);
+int scft_batch_get_densities(scft_batch *b, int instance, double *phi13, double *phi_tot);
+/* Iterate every instance until it converges or has run max_iter iterations in
+ * this call, chunk (<= SCFT_HIST_CAP) iterations per group per round. res: NULL
+ * or n results. */
+int scft_batch_run(scft_batch *b, int max_iter, int chunk, scft_batch_result *res);
 
 /* Download fields (w14 layout), the 13 total densities (13*M, field order) and
  * phi_tot (M). Any pointer may be NULL. */

@@ -90,7 +90,12 @@ class COptions(C.Structure):
 
 class CIterOut(C.Structure):
     _fields_ = [("iter", C.c_ulong), ("free_energy", D), ("rms", D), ("mf", D), ("mu", D * NSP), ("q", D * NSP),
-                ("status", C.c_int), ("pad", C.c_int)]
+                ("status", C.c_int), ("converged", C.c_int)]
+
+
+class CBatchResult(C.Structure):
+    _fields_ = [("iterations", C.c_ulong), ("iter", C.c_ulong), ("free_energy", D), ("rms", D),
+                ("converged", C.c_int), ("status", C.c_int)]
 
 
 class CTiming(C.Structure):
@@ -125,6 +130,24 @@ def lib() -> C.CDLL:
         "scft_set_rng": (I, [VP, I, us3]),
         "scft_get_rng": (I, [VP, I, us3]),
         "scft_iterate": (I, [VP, I, dp, P(CIterOut)]),
+        "scft_set_stop": (I, [VP, I, D]),
+        "scft_freeze": (I, [VP, I]),
+        "scft_set_surface": (I, [VP, I, P(CSurface)]),
+        "scft_iterate_async": (I, [VP, I]),
+        "scft_iterate_wait": (I, [VP, P(CIterOut)]),
+        "scft_batch_create": (I, [P(CSurface), I, P(COptions), P(VP)]),
+        "scft_batch_destroy": (I, [VP]),
+        "scft_batch_groups": (I, [VP]),
+        "scft_batch_locate": (I, [VP, I, P(I), P(I)]),
+        "scft_batch_context": (VP, [VP, I]),
+        "scft_batch_set_fields": (I, [VP, I, dp]),
+        "scft_batch_set_masks": (I, [VP, I, dp]),
+        "scft_batch_set_iteration": (I, [VP, I, UL]),
+        "scft_batch_set_rng": (I, [VP, I, us3]),
+        "scft_batch_set_stop": (I, [VP, I, D]),
+        "scft_batch_get_fields": (I, [VP, I, dp]),
+        "scft_batch_get_densities": (I, [VP, I, dp, dp]),
+        "scft_batch_run": (I, [VP, I, I, P(CBatchResult)]),
         "scft_get_fields": (I, [VP, I, dp]),
         "scft_get_densities": (I, [VP, I, dp, dp]),
         "scft_set_fields_all": (I, [VP, dp]),
@@ -175,5 +198,5 @@ def check(code: int, where: str) -> None:
         raise ScftError(code, where)
 
 
-__all__ = ["lib", "CSurface", "CDerived", "COptions", "CIterOut", "CTiming", "check", "ScftError", "FIELDS",
+__all__ = ["lib", "CSurface", "CDerived", "COptions", "CIterOut", "CTiming", "CBatchResult", "check", "ScftError", "FIELDS",
            "PREC_FP64", "PREC_FP32", "exported_symbols"]

@@ -7,7 +7,10 @@
  *   for s in 0 .. maxlen-2: one pass per grid axis over every active chain
  *   iter_end   (Q, densities, fused update, finalize, p shift)
  * on the context's own stream; with use_graph the sequence is captured once
- * and replayed. Every instance of a context shares grid and contour counts.
+ * and replayed. Every instance of a context shares the grid, the MASK setting
+ * and which species are present; contour counts (NS), box lengths, chi, G1 and
+ * noise amplitudes may differ. Instances with the same diffusion factors share
+ * one set of operator tables.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -47,7 +50,16 @@ struct Axis {
     int tile;
     int ntiles;
     int h, even;
-    void *spec, *tw, *kA, *kB; /* device arrays in the context's precision */
+    int dirichlet_dense; /* 1: dense operator (Dirichlet or a length with other prime factors) */
+    int dirichlet;       /* 1: the MASK 1 z axis */
+    int src;             /* grid axis 0, 1, 2 */
+};
+
+/* Propagator chains of one instance in the reference's order of species:
+ * homopolymers (one chain each), diblocks (forward and complementary), brushes
+ * (forward from the mask, complementary from ones). */
+struct ChainSpec {
+    int len, f0, f1, seg_end, init, init_arg;
 };
 
 struct scft_ctx {
@@ -63,13 +75,19 @@ struct scft_ctx {
     int nx = 0, ny = 0, nz = 0;
     int nchains = 0, nblocks = 0, maxlen = 0;
     unsigned field_use = 0;
-    std::vector<ChainDesc> chains_h; /* [B * nchains] */
-    std::vector<BlockDesc> blocks_h;
-    SpeciesDesc species_h[SCFT_NSPECIES];
+    std::vector<ChainDesc> chains_h;   /* [B * nchains] */
+    std::vector<BlockDesc> blocks_h;   /* [B * nblocks] */
+    std::vector<SpeciesDesc> species_h; /* [B * 17] */
     std::vector<Axis> axes;
+    /* operator tables: one InstOps per distinct (alphax, alphay, alphaz) */
+    std::vector<InstOps> ops_h;
+    std::vector<int> ops_of; /* [B]: index into ops_h */
+    std::vector<double> ops_alpha; /* [3 * sets]: alphax, alphay, alphaz of each set */
+    InstOps *ops = nullptr;  /* device, room for SCFT_OPS_CAP sets */
+    std::vector<int> cap;    /* [B * nchains]: contour slices allocated per chain */
+    std::vector<ChainSpec> cs0; /* instance 0's chains: the composition every instance shares */
     /* fused 2D contour step (scft_step2d.cu) */
     int fused2d = 0;
-    void *kz_rm = nullptr, *twx = nullptr, *ex = nullptr;
     int *order = nullptr; /* chain indices, longest first */
     /* device noise replay (SCFT_NOISE_DRAND48) */
     unsigned long long *rng_in = nullptr;
@@ -85,8 +103,10 @@ struct scft_ctx {
     BlockDesc *blocks = nullptr;
     SpeciesDesc *species = nullptr;
     scft_iter_out *hist = nullptr;
+    scft_iter_out *last = nullptr;      /* [B] latest record per instance */
     scft_iter_out *hist_host = nullptr; /* pinned */
     int hist_cap = 0;
+    int pending = 0; /* iterations enqueued and not yet collected */
     int nparts = 0;
     size_t device_bytes = 0;
     std::vector<void *> allocs;
@@ -103,6 +123,9 @@ struct scft_ctx {
     scft_timing last_timing{};
     long launches_per_iter = 0, prop_launches_per_iter = 0;
 };
+
+/* operator sets a context can hold (scft_set_surface may add sets) */
+#define SCFT_OPS_CAP 256
 
 static int dalloc(scft_ctx *c, void **p, size_t bytes)
 {
@@ -264,14 +287,10 @@ static int pick_tile(long lines_per_chain, long inner_or_lines, int total_chains
     return tile;
 }
 
-/* The fused 2D step: z operator rows (A then B, row-major), the four-step
- * twiddles along x and the x factor E(k)/NX. */
-static int build_fused2d(scft_ctx *c)
+/* z operator halves and x factor of one operator set for the fused 2D step. */
+static int fused2d_tables(scft_ctx *c, const scft_derived &d, InstOps &o)
 {
-    const scft_derived &d = c->der[0];
-    if (c->opt.kernel_path != 0 || d.ny != 1 || d.nx < 2 || d.nz < 2) return SCFT_OK;
-    if (scft_step2d_smem(c->opt.precision, d.nx, d.nz) == 0) return SCFT_OK;
-    const int nz = d.nz, h = nz / 2, nx = d.nx, n1 = scft_step2d_n1(nx), n2 = nx / n1;
+    const int nz = d.nz, h = nz / 2, nx = d.nx;
     std::vector<long double> K;
     dense_operator(nz, d.alphaz, c->surf[0].mask, K);
     std::vector<double> kz((size_t)2 * h * h);
@@ -288,135 +307,251 @@ static int build_fused2d(scft_ctx *c)
         std::copy(Ah.begin(), Ah.end(), kz.begin());
         std::copy(Bh.begin(), Bh.end(), kz.begin() + (size_t)h * h);
     }
-    std::vector<double> twx(2 * (size_t)nx), ex(nx);
+    std::vector<double> ex(nx);
+    for (int k = 0; k < nx; ++k) {
+        const double kk = kval(k, nx);
+        ex[k] = exp(-d.alphax * kk * kk) / nx;
+    }
+    void *kz_d = nullptr, *ex_d = nullptr;
+    int rc = upload_p(c, &kz_d, kz);
+    if (!rc) rc = upload_p(c, &ex_d, ex);
+    if (rc) return rc;
+    o.kz = kz_d;
+    o.ex = ex_d;
+    return SCFT_OK;
+}
+
+/* The fused 2D step: z operator rows (A then B, row-major) and the x factor
+ * E(k)/NX per operator set, the four-step twiddles along x once. */
+static int build_fused2d(scft_ctx *c)
+{
+    const scft_derived &d0 = c->der[0];
+    if (c->opt.kernel_path != 0 || d0.ny != 1 || d0.nx < 2 || d0.nz < 2) return SCFT_OK;
+    if (scft_step2d_smem(c->opt.precision, d0.nx, d0.nz) == 0) return SCFT_OK;
+    const int nx = d0.nx, n1 = scft_step2d_n1(nx), n2 = nx / n1;
+    std::vector<double> twx(2 * (size_t)nx);
     for (int q2 = 0; q2 < n2; ++q2)
         for (int k1 = 0; k1 < n1; ++k1) {
             const double ang = 2.0 * M_PI * (double)((q2 * k1) % nx) / nx;
             twx[2 * (q2 * n1 + k1)] = cos(ang);
             twx[2 * (q2 * n1 + k1) + 1] = -sin(ang);
         }
-    for (int k = 0; k < nx; ++k) {
-        const double kk = kval(k, nx);
-        ex[k] = exp(-d.alphax * kk * kk) / nx;
-    }
-    int rc = upload_p(c, &c->kz_rm, kz);
-    if (!rc) rc = upload_p(c, &c->twx, twx);
-    if (!rc) rc = upload_p(c, &c->ex, ex);
+    void *twx_d = nullptr;
+    int rc = upload_p(c, &twx_d, twx);
     if (rc) return rc;
+    for (size_t u = 0; u < c->ops_h.size(); ++u) {
+        int b = 0;
+        while (c->ops_of[b] != (int)u) ++b;
+        rc = fused2d_tables(c, c->der[b], c->ops_h[u]);
+        if (rc) return rc;
+        c->ops_h[u].twx = twx_d;
+    }
     Step2DArgs a;
     memset(&a, 0, sizeof(a));
-    CK(scft_launch_step2d(c->opt.precision, nx, nz, a, 0, c->stream, 1));
+    CK(scft_launch_step2d(c->opt.precision, nx, d0.nz, a, 0, c->stream, 1));
     c->fused2d = 1;
     return SCFT_OK;
 }
+/* Operator tables of one grid axis (pass slot ai) for one operator set. */
+static int axis_tables(scft_ctx *c, const Axis &A, double alpha, InstOps &o, int ai)
+{
+    const int n = A.g.n;
+    if (!A.dirichlet_dense) {
+        std::vector<double> spec(n), tw(2 * n);
+        for (int t = 0; t < n; ++t) {
+            const double k = kval(t, n);
+            spec[t] = exp(-alpha * k * k) / n;
+            tw[2 * t] = cos(2.0 * M_PI * t / n);
+            tw[2 * t + 1] = -sin(2.0 * M_PI * t / n);
+        }
+        void *sp = nullptr, *twd = nullptr;
+        int rc = upload_p(c, &sp, spec);
+        if (!rc) rc = upload_p(c, &twd, tw);
+        if (rc) return rc;
+        o.spec[ai] = sp;
+        o.tw[ai] = twd;
+        return SCFT_OK;
+    }
+    std::vector<long double> K;
+    dense_operator(n, alpha, A.dirichlet, K);
+    if (A.even) {
+        const int h = n / 2;
+        std::vector<double> Ar((size_t)h * h), Br((size_t)h * h), At((size_t)h * h), Bt((size_t)h * h);
+        for (int i = 0; i < h; ++i)
+            for (int j = 0; j < h; ++j) {
+                const long double kij = K[(size_t)i * n + j], kim = K[(size_t)i * n + (n - 1 - j)];
+                Ar[(size_t)i * h + j] = (double)((kij + kim) / 2.0L);
+                Br[(size_t)i * h + j] = (double)((kij - kim) / 2.0L);
+            }
+        if (c->psize == 4) {
+            Ar = round_fp32_colsum(Ar, h, h);
+            Br = round_fp32_colsum(Br, h, h);
+        }
+        for (int i = 0; i < h; ++i)
+            for (int j = 0; j < h; ++j) {
+                At[(size_t)j * h + i] = Ar[(size_t)i * h + j];
+                Bt[(size_t)j * h + i] = Br[(size_t)i * h + j];
+            }
+        void *ka = nullptr, *kb = nullptr;
+        int rc = upload_p(c, &ka, At);
+        if (!rc) rc = upload_p(c, &kb, Bt);
+        if (rc) return rc;
+        o.kA[ai] = ka;
+        o.kB[ai] = kb;
+    } else {
+        std::vector<double> Kt((size_t)n * n);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) Kt[(size_t)j * n + i] = (double)K[(size_t)i * n + j];
+        void *ka = nullptr;
+        int rc = upload_p(c, &ka, Kt);
+        if (rc) return rc;
+        o.kA[ai] = ka;
+        o.kB[ai] = ka;
+    }
+    return SCFT_OK;
+}
 
+/* Per-axis pass geometry (shared by every instance) and each operator set's
+ * tables. Instances with equal (alphax, alphay, alphaz) share one set. */
 static int build_axes(scft_ctx *c)
 {
     const scft_derived &d = c->der[0];
     const int dims[3] = {d.nx, d.ny, d.nz};
-    const double alphas[3] = {d.alphax, d.alphay, d.alphaz};
     const int total_chains = c->B * c->nchains;
+    c->ops_of.assign(c->B, 0);
+    c->ops_h.clear();
+    std::vector<int> rep; /* first instance of each operator set */
+    for (int b = 0; b < c->B; ++b) {
+        const scft_derived &db = c->der[b];
+        int u = 0;
+        for (; u < (int)rep.size(); ++u) {
+            const scft_derived &dr = c->der[rep[u]];
+            if (dr.alphax == db.alphax && dr.alphay == db.alphay && dr.alphaz == db.alphaz) break;
+        }
+        if (u == (int)rep.size()) {
+            rep.push_back(b);
+            c->ops_alpha.insert(c->ops_alpha.end(), {db.alphax, db.alphay, db.alphaz});
+            InstOps o;
+            memset(&o, 0, sizeof(o));
+            c->ops_h.push_back(o);
+        }
+        c->ops_of[b] = u;
+    }
+    int optin_limit = 0;
+    CK(cudaDeviceGetAttribute(&optin_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     for (int ax = 0; ax < 3; ++ax) {
         const int n = dims[ax];
         if (n <= 1) continue;
         Axis A;
         memset(&A, 0, sizeof(A));
+        A.src = ax;
         A.g.n = n;
         A.g.ls = ax == 0 ? d.ny * d.nz : (ax == 1 ? d.nz : 1);
         A.g.inner = ax == 2 ? 1 : A.g.ls;
         A.g.outer = ax == 0 ? 1 : (ax == 1 ? d.nx : d.nx * d.ny);
-        const int dirichlet = (ax == 2 && c->surf[0].mask);
-        int fft_ok = !dirichlet && radices(n, A.g.rad, &A.g.nrad);
+        A.dirichlet = (ax == 2 && c->surf[0].mask);
+        const int fft_ok = !A.dirichlet && radices(n, A.g.rad, &A.g.nrad);
         A.g.dirichlet = fft_ok ? 0 : 1;
+        A.dirichlet_dense = !fft_ok;
         const long lines = c->m / n;
         const long divisor = ax == 2 ? lines : A.g.inner;
         if (fft_ok) {
             A.tile = pick_tile(lines, divisor, total_chains, c->sms, c->psize == 8 ? 16 : 32);
-            std::vector<double> spec(n), tw(2 * n);
-            for (int t = 0; t < n; ++t) {
-                const double k = kval(t, n);
-                spec[t] = exp(-alphas[ax] * k * k) / n;
-                tw[2 * t] = cos(2.0 * M_PI * t / n);
-                tw[2 * t + 1] = -sin(2.0 * M_PI * t / n);
-            }
-            int rc = upload_p(c, &A.spec, spec);
-            if (!rc) rc = upload_p(c, &A.tw, tw);
-            if (rc) return rc;
         } else {
             A.tile = pick_tile(lines, divisor, total_chains, c->sms, c->psize == 8 ? 8 : 16);
-            std::vector<long double> K;
-            dense_operator(n, alphas[ax], dirichlet, K);
             A.even = (n % 2 == 0);
-            if (A.even) {
-                const int h = n / 2;
-                A.h = h;
-                std::vector<double> Ar((size_t)h * h), Br((size_t)h * h), At((size_t)h * h), Bt((size_t)h * h);
-                for (int i = 0; i < h; ++i)
-                    for (int j = 0; j < h; ++j) {
-                        const long double kij = K[(size_t)i * n + j], kim = K[(size_t)i * n + (n - 1 - j)];
-                        Ar[(size_t)i * h + j] = (double)((kij + kim) / 2.0L);
-                        Br[(size_t)i * h + j] = (double)((kij - kim) / 2.0L);
-                    }
-                if (c->psize == 4) {
-                    Ar = round_fp32_colsum(Ar, h, h);
-                    Br = round_fp32_colsum(Br, h, h);
-                }
-                for (int i = 0; i < h; ++i)
-                    for (int j = 0; j < h; ++j) {
-                        At[(size_t)j * h + i] = Ar[(size_t)i * h + j];
-                        Bt[(size_t)j * h + i] = Br[(size_t)i * h + j];
-                    }
-                int rc = upload_p(c, &A.kA, At);
-                if (!rc) rc = upload_p(c, &A.kB, Bt);
-                if (rc) return rc;
-            } else {
-                A.h = n;
-                std::vector<double> Kt((size_t)n * n);
-                for (int i = 0; i < n; ++i)
-                    for (int j = 0; j < n; ++j) Kt[(size_t)j * n + i] = (double)K[(size_t)i * n + j];
-                int rc = upload_p(c, &A.kA, Kt);
-                if (rc) return rc;
-                A.kB = A.kA;
-            }
+            A.h = A.even ? n / 2 : n;
         }
         const size_t smem = scft_pass_smem_bytes(A.g, A.tile, A.h, c->psize);
-        int optin_limit = 0;
-        cudaDeviceGetAttribute(&optin_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
         if (smem > (size_t)optin_limit) {
             set_err("axis %d of length %d needs %zu bytes of shared memory", ax, n, smem);
             return SCFT_ERR_PARAM;
         }
         A.ntiles = (int)(lines / A.tile);
+        const int ai = (int)c->axes.size();
+        for (size_t u = 0; u < rep.size(); ++u) {
+            const scft_derived &dr = c->der[rep[u]];
+            const double alpha = ax == 0 ? dr.alphax : (ax == 1 ? dr.alphay : dr.alphaz);
+            int rc = axis_tables(c, A, alpha, c->ops_h[u], ai);
+            if (rc) return rc;
+        }
         c->axes.push_back(A);
     }
     /* the limit is a cap, not a reservation: set the device maximum once */
-    int optin = 0;
-    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-    CK(scft_pass_configure(optin));
+    CK(scft_pass_configure(optin_limit));
     return SCFT_OK;
 }
 
-/* Check that every instance has the same shape as instance 0. */
+/* Instances of one context share the grid, the MASK setting and the active
+ * field set (the noise layout); the species composition is compared after the
+ * chains are built. */
 static int same_shape(const scft_surface &a, const scft_derived &da, const scft_surface &b, const scft_derived &db)
 {
-    if (da.nx != db.nx || da.ny != db.ny || da.nz != db.nz || a.mask != b.mask || a.ns != b.ns) return 0;
-    if (memcmp(da.ns_dbk, db.ns_dbk, sizeof(da.ns_dbk)) || memcmp(da.ns_dbk_x, db.ns_dbk_x, sizeof(da.ns_dbk_x)) ||
-        memcmp(da.ns_homo, db.ns_homo, sizeof(da.ns_homo)) || memcmp(da.ns_s, db.ns_s, sizeof(da.ns_s)))
-        return 0;
-    if (da.alphax != db.alphax || da.alphay != db.alphay || da.alphaz != db.alphaz) return 0;
-    if (a.enable_seed != b.enable_seed || da.n_active != db.n_active || memcmp(da.active, db.active, sizeof(da.active)))
-        return 0;
+    if (da.nx != db.nx || da.ny != db.ny || da.nz != db.nz || a.mask != b.mask) return 0;
+    if (da.n_active != db.n_active || memcmp(da.active, db.active, sizeof(da.active))) return 0;
     return 1;
 }
 
-static void fill_params(const scft_surface &s, const scft_derived &d, const std::vector<BlockDesc> &blocks,
+/* Chains, density blocks and species table of one instance (see ChainSpec). */
+static void build_instance(const scft_surface &s, const scft_derived &d, std::vector<ChainSpec> &cs,
+                           std::vector<BlockDesc> &blocks, SpeciesDesc *species)
+{
+    cs.clear();
+    blocks.clear();
+    memset(species, 0, sizeof(SpeciesDesc) * SCFT_NSPECIES);
+    for (int h = 0; h < 10; ++h) {
+        if (d.ns_homo[h] <= 0) continue;
+        const int ci = (int)cs.size();
+        cs.push_back({d.ns_homo[h], h, h, d.ns_homo[h], SCFT_INIT_ONES, 0});
+        blocks.push_back({ci, ci, 0, d.ns_homo[h] - 1, d.ns_homo[h], 4 + h, h, 1});
+        species[4 + h] = {1, ci, d.ns_homo[h], 0};
+    }
+    for (int k = 0; k < 4; ++k) {
+        if (!(s.vol_dbk[k] > 0.0)) continue;
+        const int fx = DBK_FX[k], fy = fx + 1, ns = d.ns_dbk[k], nx_ = d.ns_dbk_x[k], ny_ = d.ns_dbk_y[k];
+        const int cf = (int)cs.size();
+        cs.push_back({ns, fx, fy, nx_ - 1, (k == 0 && s.enable_seed == 1) ? SCFT_INIT_SEED : SCFT_INIT_ONES, 0});
+        const int cb = (int)cs.size();
+        cs.push_back({ns, fy, fx, ny_, SCFT_INIT_ONES, 0});
+        blocks.push_back({cf, cb, 0, nx_ - 1, ns, k, fx, 0});
+        blocks.push_back({cf, cb, nx_ - 1, ns - 1, ns, k, fy, 0});
+        /* Q from the complementary chain for dbk1/2, the forward chain for dbk3/4 (SCFT.c:1271, :1314, :1357, :1399) */
+        species[k] = {1, k < 2 ? cb : cf, ns, 0};
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (d.ns_s[k] <= 0) continue;
+        const int ns = d.ns_s[k];
+        const int cf = (int)cs.size();
+        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_MASK, k});
+        const int cb = (int)cs.size();
+        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_ONES, 0});
+        blocks.push_back({cf, cb, 0, ns - 1, ns, 14 + k, 10 + k, 0});
+        species[14 + k] = {1, cf, ns, 0};
+    }
+}
+
+/* Same chains and blocks up to contour counts: equal fields, species and parts. */
+static int same_composition(const std::vector<ChainSpec> &ca, const std::vector<BlockDesc> &ba,
+                            const std::vector<ChainSpec> &cb, const std::vector<BlockDesc> &bb)
+{
+    if (ca.size() != cb.size() || ba.size() != bb.size()) return 0;
+    for (size_t k = 0; k < ca.size(); ++k)
+        if (ca[k].f0 != cb[k].f0 || ca[k].f1 != cb[k].f1) return 0;
+    for (size_t k = 0; k < ba.size(); ++k)
+        if (ba[k].species != bb[k].species || ba[k].field != bb[k].field || ba[k].part != bb[k].part ||
+            ba[k].chain_f != bb[k].chain_f || ba[k].chain_b != bb[k].chain_b)
+            return 0;
+    return 1;
+}
+
+static void fill_params(const scft_surface &s, const scft_derived &d, const BlockDesc *blocks, int nblocks,
                         const SpeciesDesc *species, InstParams &ip)
 {
     memset(&ip, 0, sizeof(ip));
     memcpy(ip.chi, d.chi_eff, sizeof(ip.chi));
     memcpy(ip.phi_avg, d.phi_avg, sizeof(ip.phi_avg));
     const double coat = d.coating_vol;
-    for (size_t k = 0; k < blocks.size(); ++k) {
+    for (int k = 0; k < nblocks; ++k) {
         const BlockDesc &bd = blocks[k];
         double frac;
         if (bd.species < 4)
@@ -507,7 +642,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
             return rc;
         }
         if (b > 0 && !same_shape(c->surf[0], c->der[0], c->surf[b], c->der[b])) {
-            set_err("instance %d differs in grid or contour counts from instance 0", b);
+            set_err("instance %d differs from instance 0 in grid, MASK or active fields", b);
             scft_ctx_destroy(c);
             return SCFT_ERR_PARAM;
         }
@@ -520,57 +655,44 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     c->m = d.m;
     c->sm = (d.m + 63) / 64 * 64;
 
-    /* chains, blocks, species (one instance's worth; identical across instances) */
-    struct ChainSpec {
-        int len, f0, f1, seg_end, init, init_arg;
-    };
-    std::vector<ChainSpec> cs;
-    std::vector<BlockDesc> blocks;
-    memset(c->species_h, 0, sizeof(c->species_h));
-    for (int h = 0; h < 10; ++h) {
-        if (d.ns_homo[h] <= 0) continue;
-        const int ci = (int)cs.size();
-        cs.push_back({d.ns_homo[h], h, h, d.ns_homo[h], SCFT_INIT_ONES, 0});
-        blocks.push_back({ci, ci, 0, d.ns_homo[h] - 1, d.ns_homo[h], 4 + h, h, 1});
-        c->species_h[4 + h] = {1, ci, d.ns_homo[h], 0};
+    /* chains, blocks, species per instance (same composition, own contour counts) */
+    std::vector<std::vector<ChainSpec>> cs(c->B);
+    std::vector<BlockDesc> blk;
+    c->species_h.assign((size_t)c->B * SCFT_NSPECIES, SpeciesDesc{});
+    for (int b = 0; b < c->B; ++b) {
+        build_instance(c->surf[b], c->der[b], cs[b], blk, &c->species_h[(size_t)b * SCFT_NSPECIES]);
+        if (b == 0) {
+            c->blocks_h = blk;
+            c->nblocks = (int)blk.size();
+            continue;
+        }
+        const std::vector<BlockDesc> b0(c->blocks_h.begin(), c->blocks_h.begin() + c->nblocks);
+        int same = same_composition(cs[0], b0, cs[b], blk);
+        for (int sp = 0; sp < SCFT_NSPECIES && same; ++sp) {
+            const SpeciesDesc &x = c->species_h[sp], &y = c->species_h[(size_t)b * SCFT_NSPECIES + sp];
+            same = x.present == y.present && x.q_chain == y.q_chain;
+        }
+        if (!same) {
+            set_err("instance %d differs from instance 0 in which species are present", b);
+            scft_ctx_destroy(c);
+            return SCFT_ERR_PARAM;
+        }
+        c->blocks_h.insert(c->blocks_h.end(), blk.begin(), blk.end());
     }
-    for (int k = 0; k < 4; ++k) {
-        if (!(s.vol_dbk[k] > 0.0)) continue;
-        const int fx = DBK_FX[k], fy = fx + 1, ns = d.ns_dbk[k], nx_ = d.ns_dbk_x[k], ny_ = d.ns_dbk_y[k];
-        const int cf = (int)cs.size();
-        cs.push_back({ns, fx, fy, nx_ - 1, (k == 0 && s.enable_seed == 1) ? SCFT_INIT_SEED : SCFT_INIT_ONES, 0});
-        const int cb = (int)cs.size();
-        cs.push_back({ns, fy, fx, ny_, SCFT_INIT_ONES, 0});
-        blocks.push_back({cf, cb, 0, nx_ - 1, ns, k, fx, 0});
-        blocks.push_back({cf, cb, nx_ - 1, ns - 1, ns, k, fy, 0});
-        /* Q from the complementary chain for dbk1/2, the forward chain for dbk3/4 (SCFT.c:1271, :1314, :1357, :1399) */
-        c->species_h[k] = {1, k < 2 ? cb : cf, ns, 0};
-    }
-    for (int k = 0; k < 3; ++k) {
-        if (d.ns_s[k] <= 0) continue;
-        const int ns = d.ns_s[k];
-        const int cf = (int)cs.size();
-        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_MASK, k});
-        const int cb = (int)cs.size();
-        cs.push_back({ns, 10 + k, 10 + k, ns, SCFT_INIT_ONES, 0});
-        blocks.push_back({cf, cb, 0, ns - 1, ns, 14 + k, 10 + k, 0});
-        c->species_h[14 + k] = {1, cf, ns, 0};
-    }
-    if (cs.empty()) {
+    if (cs[0].empty()) {
         set_err("no species with a positive volume fraction");
         scft_ctx_destroy(c);
         return SCFT_ERR_PARAM;
     }
-    c->nchains = (int)cs.size();
-    c->nblocks = (int)blocks.size();
-    c->blocks_h = blocks;
+    c->nchains = (int)cs[0].size();
     c->maxlen = 0;
     c->field_use = 0;
-    for (const ChainSpec &x : cs) {
-        if (x.len > c->maxlen) c->maxlen = x.len;
-        c->field_use |= 1u << x.f0;
-        c->field_use |= 1u << x.f1;
-    }
+    for (int b = 0; b < c->B; ++b)
+        for (const ChainSpec &x : cs[b]) {
+            if (x.len > c->maxlen) c->maxlen = x.len;
+            c->field_use |= 1u << x.f0;
+            c->field_use |= 1u << x.f1;
+        }
 
     int rc = SCFT_OK;
     const long sm = c->sm;
@@ -593,18 +715,52 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     c->nparts = scft_post_nparts(c->m, c->sms);
     ALLOC(c->partial, sizeof(double) * B * SCFT_NSPECIES * c->nparts);
     ALLOC(c->noise, sizeof(double) * B * d.n_active * sm);
-    c->hist_cap = 256;
+    c->hist_cap = SCFT_HIST_CAP;
     ALLOC(c->hist, sizeof(scft_iter_out) * c->hist_cap * B);
+    ALLOC(c->last, sizeof(scft_iter_out) * B);
     if (cudaMallocHost((void **)&c->hist_host, sizeof(scft_iter_out) * c->hist_cap * B) != cudaSuccess) {
         set_err("cudaMallocHost failed");
         scft_ctx_destroy(c);
         return SCFT_ERR_OOM;
     }
+#undef ALLOC
+    if ((rc = build_axes(c)) || (rc = build_fused2d(c))) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
+    if ((int)c->ops_h.size() > SCFT_OPS_CAP) {
+        set_err("more than %d distinct operator sets in one context", SCFT_OPS_CAP);
+        scft_ctx_destroy(c);
+        return SCFT_ERR_PARAM;
+    }
+    rc = dalloc(c, (void **)&p, sizeof(InstOps) * SCFT_OPS_CAP);
+    if (rc) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
+    c->ops = (InstOps *)p;
+    if (cudaMemcpyAsync(c->ops, c->ops_h.data(), sizeof(InstOps) * c->ops_h.size(), cudaMemcpyHostToDevice,
+                        c->stream) != cudaSuccess) {
+        set_err("operator upload failed");
+        scft_ctx_destroy(c);
+        return SCFT_ERR_CUDA;
+    }
+    c->cs0 = cs[0];
+#define ALLOC(ptr, bytes)                                    \
+    do {                                                     \
+        rc = dalloc(c, &p, (bytes));                         \
+        if (rc) {                                            \
+            scft_ctx_destroy(c);                             \
+            return rc;                                       \
+        }                                                    \
+        ptr = (decltype(ptr))p;                              \
+    } while (0)
     c->chains_h.resize((size_t)B * c->nchains);
     for (int b = 0; b < B; ++b)
         for (int k = 0; k < c->nchains; ++k) {
-            const ChainSpec &x = cs[k];
+            const ChainSpec &x = cs[b][k];
             ChainDesc &cd = c->chains_h[(size_t)b * c->nchains + k];
+            memset(&cd, 0, sizeof(cd));
             void *q, *t;
             ALLOC(q, (size_t)c->psize * x.len * sm);
             ALLOC(t, (size_t)c->psize * sm);
@@ -617,17 +773,15 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
             cd.init = x.init;
             cd.init_arg = x.init_arg;
             cd.instance = b;
-            cd.pad = 0;
+            cd.ops = c->ops + c->ops_of[b];
+            c->cap.push_back(x.len);
         }
     std::vector<InstParams> ip(B);
-    for (int b = 0; b < B; ++b) fill_params(c->surf[b], c->der[b], c->blocks_h, c->species_h, ip[b]);
+    for (int b = 0; b < B; ++b)
+        fill_params(c->surf[b], c->der[b], &c->blocks_h[(size_t)b * c->nblocks], c->nblocks,
+                    &c->species_h[(size_t)b * SCFT_NSPECIES], ip[b]);
     if ((rc = upload(c, (void **)&c->params, ip)) || (rc = upload(c, (void **)&c->chains, c->chains_h)) ||
-        (rc = upload(c, (void **)&c->blocks, c->blocks_h))) {
-        scft_ctx_destroy(c);
-        return rc;
-    }
-    std::vector<SpeciesDesc> spv(c->species_h, c->species_h + SCFT_NSPECIES);
-    if ((rc = upload(c, (void **)&c->species, spv))) {
+        (rc = upload(c, (void **)&c->blocks, c->blocks_h)) || (rc = upload(c, (void **)&c->species, c->species_h))) {
         scft_ctx_destroy(c);
         return rc;
     }
@@ -645,10 +799,6 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         }
     }
 #undef ALLOC
-    if ((rc = build_axes(c)) || (rc = build_fused2d(c))) {
-        scft_ctx_destroy(c);
-        return rc;
-    }
     {
         /* longest chains first, so the persistent launch ends with short ones */
         std::vector<int> ord((size_t)B * c->nchains);
@@ -711,7 +861,131 @@ extern "C" int scft_set_iteration(scft_ctx *c, int b, unsigned long it)
     if (!c || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
     c->iter[b] = it;
+    static const int zero = 0;
     CK(cudaMemcpyAsync(&c->state[b].iter, &c->iter[b], sizeof(unsigned long), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(&c->state[b].done, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_freeze(scft_ctx *c, int b)
+{
+    if (!c || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    if (c->pending) return SCFT_ERR_STATE;
+    cudaSetDevice(c->device);
+    static const int one = 1;
+    CK(cudaMemcpyAsync(&c->state[b].done, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+/* Operator tables of a new operator set (per-axis passes and, where the
+ * context uses it, the fused 2D step). */
+static int build_opset(scft_ctx *c, const scft_derived &d, InstOps &o)
+{
+    memset(&o, 0, sizeof(o));
+    for (size_t ai = 0; ai < c->axes.size(); ++ai) {
+        const Axis &A = c->axes[ai];
+        const double alpha = A.src == 0 ? d.alphax : (A.src == 1 ? d.alphay : d.alphaz);
+        int rc = axis_tables(c, A, alpha, o, (int)ai);
+        if (rc) return rc;
+    }
+    if (c->fused2d) {
+        int rc = fused2d_tables(c, d, o);
+        if (rc) return rc;
+        o.twx = c->ops_h[0].twx;
+    }
+    return SCFT_OK;
+}
+
+extern "C" int scft_set_surface(scft_ctx *c, int b, const scft_surface *s)
+{
+    if (!c || !s || b < 0 || b >= c->B) return SCFT_ERR_PARAM;
+    if (c->pending) {
+        set_err("scft_set_surface while iterations are in flight");
+        return SCFT_ERR_STATE;
+    }
+    cudaSetDevice(c->device);
+    scft_derived d;
+    int rc = scft_derive(s, &d);
+    if (rc != SCFT_OK) {
+        set_err("parameter derivation failed (%d)", rc);
+        return rc;
+    }
+    if (!same_shape(c->surf[0], c->der[0], *s, d)) {
+        set_err("the surface differs from the context in grid, MASK or active fields");
+        return SCFT_ERR_PARAM;
+    }
+    std::vector<ChainSpec> cs;
+    std::vector<BlockDesc> blk;
+    SpeciesDesc sp[SCFT_NSPECIES];
+    build_instance(*s, d, cs, blk, sp);
+    const std::vector<BlockDesc> b0(c->blocks_h.begin(), c->blocks_h.begin() + c->nblocks);
+    int same = same_composition(c->cs0, b0, cs, blk);
+    for (int k = 0; k < SCFT_NSPECIES && same; ++k)
+        same = c->species_h[k].present == sp[k].present && c->species_h[k].q_chain == sp[k].q_chain;
+    if (!same) {
+        set_err("the surface differs from the context in which species are present");
+        return SCFT_ERR_PARAM;
+    }
+    for (int k = 0; k < c->nchains; ++k)
+        if (cs[k].len > c->cap[(size_t)b * c->nchains + k]) {
+            set_err("chain %d needs %d contour slices; slot %d holds %d", k, cs[k].len, b,
+                    c->cap[(size_t)b * c->nchains + k]);
+            return SCFT_ERR_PARAM;
+        }
+    /* operator set: reuse one with the same diffusion factors, else add one */
+    int u = 0;
+    for (; u < (int)c->ops_h.size(); ++u) {
+        const double *al = &c->ops_alpha[3 * (size_t)u];
+        if (al[0] == d.alphax && al[1] == d.alphay && al[2] == d.alphaz) break;
+    }
+    if (u == (int)c->ops_h.size()) {
+        if (u >= SCFT_OPS_CAP) {
+            set_err("operator-set capacity (%d) of the context is used up", SCFT_OPS_CAP);
+            return SCFT_ERR_PARAM;
+        }
+        InstOps o;
+        rc = build_opset(c, d, o);
+        if (rc) return rc;
+        c->ops_h.push_back(o);
+        c->ops_alpha.insert(c->ops_alpha.end(), {d.alphax, d.alphay, d.alphaz});
+        CK(cudaMemcpyAsync(c->ops + u, &o, sizeof(InstOps), cudaMemcpyHostToDevice, c->stream));
+    }
+    c->ops_of[b] = u;
+    for (int k = 0; k < c->nchains; ++k) {
+        ChainDesc &cd = c->chains_h[(size_t)b * c->nchains + k];
+        cd.seg_end = cs[k].seg_end;
+        cd.len = cs[k].len;
+        cd.init = cs[k].init;
+        cd.init_arg = cs[k].init_arg;
+        cd.ops = c->ops + u;
+    }
+    std::copy(blk.begin(), blk.end(), c->blocks_h.begin() + (size_t)b * c->nblocks);
+    std::copy(sp, sp + SCFT_NSPECIES, c->species_h.begin() + (size_t)b * SCFT_NSPECIES);
+    c->surf[b] = *s;
+    c->der[b] = d;
+    InstParams ip;
+    fill_params(*s, d, blk.data(), c->nblocks, sp, ip);
+    std::vector<int> ord((size_t)c->B * c->nchains);
+    for (size_t k = 0; k < ord.size(); ++k) ord[k] = (int)k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return c->chains_h[x].len > c->chains_h[y].len; });
+    CK(cudaMemcpyAsync(c->params + b, &ip, sizeof(ip), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->chains + (size_t)b * c->nchains, &c->chains_h[(size_t)b * c->nchains],
+                       sizeof(ChainDesc) * c->nchains, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->blocks + (size_t)b * c->nblocks, blk.data(), sizeof(BlockDesc) * c->nblocks,
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->species + (size_t)b * SCFT_NSPECIES, sp, sizeof(sp), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->order, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SCFT_OK;
+}
+
+extern "C" int scft_set_stop(scft_ctx *c, int b, double rms_tol)
+{
+    if (!c || b < 0 || b >= c->B || !(rms_tol >= 0.0)) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(&c->state[b].stop_rms, &rms_tol, sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
 }
@@ -773,6 +1047,7 @@ static PostArgs post_args(scft_ctx *c, const double *noise_dev)
     a.nparts = c->nparts;
     a.noise = noise_dev;
     a.hist = c->hist;
+    a.last = c->last;
     a.hist_cap = c->hist_cap;
     for (int f = 0; f < SCFT_NFIELDS; ++f) a.part0[f] = a.part1[f] = -1;
     for (int k = 0; k < c->nblocks; ++k) {
@@ -793,12 +1068,10 @@ static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total,
         Step2DArgs a;
         a.chains = chains;
         a.order = (chains == c->chains) ? c->order : nullptr;
+        a.state = (chains == c->chains) ? c->state : nullptr;
         a.s = 0;
         a.s_end = maxlen - 1;
         a.sstride = c->sm;
-        a.kz = c->kz_rm;
-        a.twx = c->twx;
-        a.ex = c->ex;
         CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0));
         return SCFT_OK;
     }
@@ -809,16 +1082,14 @@ static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total,
             PassArgs pa;
             memset(&pa, 0, sizeof(pa));
             pa.chains = chains;
+            pa.state = (chains == c->chains) ? c->state : nullptr;
             pa.nchains = nchains_total;
             pa.s = s;
             pa.first = pi == 0;
             pa.last = pi == npass - 1;
             pa.tile = A.tile;
             pa.sstride = c->sm;
-            pa.spec = A.spec;
-            pa.tw = A.tw;
-            pa.kA = A.kA;
-            pa.kB = A.kB;
+            pa.axis = pi;
             pa.h = A.h;
             pa.even = A.even;
             CK(scft_launch_pass(c->opt.precision, A.g, pa, A.ntiles, c->stream));
@@ -857,15 +1128,100 @@ static int launch_iteration(scft_ctx *c, const double *noise_dev, int slot)
     return SCFT_OK;
 }
 
-extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_out *out)
+/* Enqueue chunk <= hist_cap iterations on the context's stream, with host
+ * noise for them ([chunk][B][n_active][M]) or NULL, and the copy of their
+ * records to pinned memory. Nothing waits. */
+static int enqueue_chunk(scft_ctx *c, int chunk, const double *noise)
 {
-    if (!c || n < 0) return SCFT_ERR_PARAM;
+    if (c->timing && c->ev.empty()) {
+        c->ev.resize(2 + 2 * c->hist_cap);
+        for (cudaEvent_t &e : c->ev) CK(cudaEventCreate(&e));
+    }
+    PostArgs a = post_args(c, nullptr);
+    CK(scft_post_mark_start(a, c->stream));
+    if (c->timing) CK(cudaEventRecord(c->ev[0], c->stream));
+    for (int k = 0; k < chunk; ++k) {
+        const double *nd = nullptr;
+        if (noise) {
+            const size_t m = (size_t)c->m, na = c->der[0].n_active;
+            for (int b = 0; b < c->B; ++b)
+                for (size_t f = 0; f < na; ++f)
+                    CK(cudaMemcpyAsync(c->noise + ((size_t)b * na + f) * c->sm,
+                                       noise + ((size_t)k * c->B * na + (size_t)b * na + f) * m, sizeof(double) * m,
+                                       cudaMemcpyHostToDevice, c->stream));
+            nd = c->noise;
+        }
+        if (c->opt.use_graph && !c->timing) {
+            if (!c->graph_exec) {
+                /* the graph always reads noise from c->noise; with no noise the
+                 * buffer holds zeros and MF*DT_NOISE == 0 skips it */
+                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                int rc = launch_iteration(c, c->noise, k);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                if (rc) return rc;
+                CK(e);
+                c->graph = g;
+                CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
+            }
+            CK(cudaGraphLaunch(c->graph_exec, c->stream));
+        } else {
+            int rc = launch_iteration(c, c->opt.noise_mode == SCFT_NOISE_DRAND48 ? c->noise : nd, k);
+            if (rc) return rc;
+        }
+    }
+    if (c->timing) CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaMemcpyAsync(c->hist_host, c->hist, sizeof(scft_iter_out) * chunk * c->B, cudaMemcpyDeviceToHost,
+                       c->stream));
+    c->pending = chunk;
+    return SCFT_OK;
+}
+
+/* Wait for the enqueued chunk; records to out ([chunk][B], may be NULL). */
+static int collect_chunk(scft_ctx *c, scft_iter_out *out)
+{
+    const int chunk = c->pending;
+    c->pending = 0;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->timing) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        c->last_timing.total_ms += ms;
+        for (int k = 0; k < chunk; ++k) {
+            float pm = 0.f;
+            cudaEventElapsedTime(&pm, c->ev[2 + 2 * k], c->ev[3 + 2 * k]);
+            c->last_timing.prop_ms += pm;
+        }
+    }
+    c->last_timing.prop_launches += (long)chunk * c->prop_launches_per_iter;
+    c->last_timing.kernel_launches += (long)chunk * c->launches_per_iter;
+    int status = SCFT_OK;
+    for (int k = 0; k < chunk; ++k)
+        for (int b = 0; b < c->B; ++b) {
+            const scft_iter_out &r = c->hist_host[(size_t)k * c->B + b];
+            if (out) out[(size_t)k * c->B + b] = r;
+            if (r.status != SCFT_OK) status = r.status;
+        }
+    if (chunk > 0)
+        for (int b = 0; b < c->B; ++b) c->iter[b] = c->hist_host[(size_t)(chunk - 1) * c->B + b].iter;
+    if (status != SCFT_OK) {
+        set_err("non-finite Q, free energy or RMS");
+        return status;
+    }
+    return SCFT_OK;
+}
+
+static int check_iterate(scft_ctx *c, int n, const double *noise)
+{
+    if (c->pending) {
+        set_err("iterations enqueued by scft_iterate_async have not been collected");
+        return SCFT_ERR_STATE;
+    }
     for (int b = 0; b < c->B; ++b)
         if (!c->fields_set[b]) {
             set_err("instance %d: scft_set_fields was not called", b);
             return SCFT_ERR_STATE;
         }
-    cudaSetDevice(c->device);
     if (noise && c->opt.noise_mode == SCFT_NOISE_DRAND48) {
         set_err("this context draws its noise on the device; pass NULL");
         return SCFT_ERR_PARAM;
@@ -882,78 +1238,53 @@ extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_o
                 }
             }
     }
-    if (c->timing && c->ev.empty()) {
-        c->ev.resize(2 + 2 * c->hist_cap);
-        for (cudaEvent_t &e : c->ev) CK(cudaEventCreate(&e));
-    }
+    return SCFT_OK;
+}
+
+extern "C" int scft_iterate(scft_ctx *c, int n, const double *noise, scft_iter_out *out)
+{
+    if (!c || n < 0) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    int rc = check_iterate(c, n, noise);
+    if (rc) return rc;
     c->last_timing = scft_timing{};
+    const size_t per_iter = (size_t)c->B * c->der[0].n_active * (size_t)c->m;
     int done = 0;
     while (done < n) {
         const int chunk = (n - done) < c->hist_cap ? (n - done) : c->hist_cap;
-        PostArgs a = post_args(c, nullptr);
-        CK(scft_post_mark_start(a, c->stream));
-        if (c->timing) CK(cudaEventRecord(c->ev[0], c->stream));
-        for (int k = 0; k < chunk; ++k) {
-            const double *nd = nullptr;
-            if (noise) {
-                const size_t m = (size_t)c->m, na = c->der[0].n_active;
-                for (int b = 0; b < c->B; ++b)
-                    for (size_t f = 0; f < na; ++f)
-                        CK(cudaMemcpyAsync(c->noise + ((size_t)b * na + f) * c->sm,
-                                           noise + ((size_t)(done + k) * c->B * na + (size_t)b * na + f) * m,
-                                           sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
-                nd = c->noise;
-            }
-            if (c->opt.use_graph && !c->timing) {
-                if (!c->graph_exec) {
-                    /* the graph always reads noise from c->noise; with no noise the
-                     * buffer holds zeros and MF*DT_NOISE == 0 skips it */
-                    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                    int rc = launch_iteration(c, c->noise, k);
-                    cudaGraph_t g = nullptr;
-                    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-                    if (rc) return rc;
-                    CK(e);
-                    c->graph = g;
-                    CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
-                }
-                CK(cudaGraphLaunch(c->graph_exec, c->stream));
-            } else {
-                int rc = launch_iteration(c, c->opt.noise_mode == SCFT_NOISE_DRAND48 ? c->noise : nd, k);
-                if (rc) return rc;
-            }
+        rc = enqueue_chunk(c, chunk, noise ? noise + (size_t)done * per_iter : nullptr);
+        if (rc) {
+            cudaStreamSynchronize(c->stream);
+            c->pending = 0;
+            return rc;
         }
-        if (c->timing) CK(cudaEventRecord(c->ev[1], c->stream));
-        CK(cudaMemcpyAsync(c->hist_host, c->hist, sizeof(scft_iter_out) * chunk * c->B, cudaMemcpyDeviceToHost,
-                           c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        if (c->timing) {
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
-            c->last_timing.total_ms += ms;
-            for (int k = 0; k < chunk; ++k) {
-                float pm = 0.f;
-                cudaEventElapsedTime(&pm, c->ev[2 + 2 * k], c->ev[3 + 2 * k]);
-                c->last_timing.prop_ms += pm;
-            }
-        }
-        c->last_timing.prop_launches += (long)chunk * c->prop_launches_per_iter;
-        c->last_timing.kernel_launches += (long)chunk * c->launches_per_iter;
-        int status = SCFT_OK;
-        for (int k = 0; k < chunk; ++k)
-            for (int b = 0; b < c->B; ++b) {
-                const scft_iter_out &r = c->hist_host[(size_t)k * c->B + b];
-                if (out) out[(size_t)(done + k) * c->B + b] = r;
-                if (r.status != SCFT_OK) status = r.status;
-            }
-        for (int b = 0; b < c->B; ++b) c->iter[b] += chunk;
+        rc = collect_chunk(c, out ? out + (size_t)done * c->B : nullptr);
+        if (rc) return rc;
         done += chunk;
-        if (status != SCFT_OK) {
-            set_err("non-finite Q, free energy or RMS");
-            return status;
-        }
     }
     return SCFT_OK;
+}
+
+extern "C" int scft_iterate_async(scft_ctx *c, int n)
+{
+    if (!c || n < 1 || n > SCFT_HIST_CAP) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    int rc = check_iterate(c, n, nullptr);
+    if (rc) return rc;
+    c->last_timing = scft_timing{};
+    rc = enqueue_chunk(c, n, nullptr);
+    if (rc) {
+        cudaStreamSynchronize(c->stream);
+        c->pending = 0;
+    }
+    return rc;
+}
+
+extern "C" int scft_iterate_wait(scft_ctx *c, scft_iter_out *out)
+{
+    if (!c) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    return collect_chunk(c, out);
 }
 
 extern "C" int scft_get_fields(scft_ctx *c, int b, double *w14)
@@ -1043,6 +1374,7 @@ extern "C" int scft_propagate(scft_ctx *c, const double *q0, const double *w, in
         cd.b1 = bzd;
         cd.seg_end = steps + 1;
         cd.len = steps + 1;
+        cd.ops = c->ops + c->ops_of[0];
         e = cudaMemcpyAsync(cdd, &cd, sizeof(cd), cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(wd, w, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(qd, q0, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream);
@@ -1093,9 +1425,11 @@ extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
 /* ------------------------------------------------- internal hooks */
 /* Used by scft_noalloc.cu: context facts and the contour-step launcher on a
  * caller-provided chain descriptor. */
-int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st)
+int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st,
+                  const InstOps **ops0)
 {
     if (!c) return SCFT_ERR_PARAM;
+    *ops0 = c->ops + c->ops_of[0];
     *device = c->device;
     *prec = c->opt.precision;
     *m = c->m;

@@ -26,6 +26,15 @@
 #define SCFT_INIT_MASK 1
 #define SCFT_INIT_SEED 2
 
+/* Diffusion operators of one instance (they depend on DS and the grid
+ * spacing, so instances with different NS or box lengths have their own):
+ * tables of the fused 2D chain kernel and, per grid axis in the context's axis
+ * order, those of the per-axis passes. Instances with equal operators share. */
+struct InstOps {
+    const void *kz, *twx, *ex;
+    const void *spec[3], *tw[3], *kA[3], *kB[3];
+};
+
 /* One propagator chain of one instance: q[0] from init, then len-1 contour
  * steps; steps s < seg_end use field f0, later steps field f1 (the diblock
  * junction). */
@@ -40,6 +49,7 @@ struct ChainDesc {
     int init_arg;   /* mask index for SCFT_INIT_MASK */
     int instance;
     int pad;
+    const InstOps *ops; /* the instance's operators (device) */
 };
 
 /* One funDensity call (SCFT.c:2270-2308) of one species block. */
@@ -79,12 +89,14 @@ struct InstParams {
 /* Per-instance device state that changes every iteration. */
 struct InstState {
     unsigned long iter;   /* iIter, incremented at the start of each iteration */
-    unsigned long iter0;  /* value at the start of the current scft_iterate call */
+    unsigned long tick;   /* iterations launched in the current scft_iterate call (history slot + 1) */
     unsigned long long rng; /* 48-bit drand48 state (device noise replay) */
     double q[SCFT_NSPECIES];
     double p_avg;
+    double stop_rms;      /* 0: run every iteration; else freeze once RMS < stop_rms */
     int status;
-    int pad;
+    int done;             /* 1: frozen, every kernel skips the instance; 2: met the stop criterion in
+                             this iteration (the p shift still runs; the next iteration begins frozen) */
 };
 
 /* Geometry of one axis pass of the propagator step. */
@@ -101,16 +113,14 @@ struct AxisGeom {
 /* Arguments of one axis pass of the propagator step (scft_prop.cu). */
 struct PassArgs {
     const ChainDesc *chains;
+    const InstState *state; /* [B]: chains of frozen instances are skipped (NULL: no check) */
     int nchains;
     int s;          /* contour step: reads slice s, writes slice s+1 */
     int first;      /* multiply by b on load, read q[s] */
     int last;       /* multiply by b on store, write q[s+1] */
     int tile;       /* lines per CTA */
     long sstride;   /* slice stride (elements) */
-    const void *spec; /* P[n]: E(k_t)/n (periodic) */
-    const void *tw;   /* Cx<P>[n] twiddles (periodic) */
-    const void *kA;   /* P[h*h] transposed, dense Dirichlet half operators */
-    const void *kB;
+    int axis;       /* operator slot in InstOps: spec/tw (periodic FFT) or kA/kB (dense) */
     int h;          /* half size (n even) or n (odd: kA holds the full matrix) */
     int even;
 };
@@ -124,8 +134,8 @@ struct PostArgs {
     const InstParams *params;   /* [B] */
     InstState *state;           /* [B] */
     const ChainDesc *chains;    /* [B * nchains] */
-    const BlockDesc *blocks;    /* [nblocks] (same for every instance) */
-    const SpeciesDesc *species; /* [17] */
+    const BlockDesc *blocks;    /* [B][nblocks] */
+    const SpeciesDesc *species; /* [B][17] */
     int nchains, nblocks;
     int B;
     int nx, ny, nz;
@@ -140,6 +150,7 @@ struct PostArgs {
     int nparts;
     const double *noise;        /* [B][n_active][sm] or NULL */
     scft_iter_out *hist;        /* [cap][B] */
+    scft_iter_out *last;        /* [B]: the latest record (repeated while frozen) */
     int hist_cap;
     /* which density blocks make up each field's total (funAddArray operands,
      * SCFT.c:1486-1495): first operand (diblock or brush block), second
@@ -159,12 +170,13 @@ cudaError_t scft_boltz_one(int prec, const double *w, void *bz, double ds, long 
 struct Step2DArgs {
     const ChainDesc *chains;
     const int *order;  /* chain indices, longest first (or NULL) */
+    const InstState *state; /* [B]: chains of frozen instances return at once (NULL: no check) */
     int s;             /* first contour step: reads slice s */
     int s_end;         /* runs steps s .. min(s_end, len-1)-1 */
     long sstride;      /* slice stride (elements) */
-    const void *kz;    /* P[2*H*H]: A[i][k] then B[i][k], H = NZ/2 */
-    const void *twx;   /* Cx<P>[NX]: exp(-2 pi i n2 k1 / NX) at n2*N1 + k1 */
-    const void *ex;    /* P[NX]: E_x(k)/NX */
+    /* per chain through ChainDesc::ops: kz P[2*H*H] (A[i][k] then B[i][k],
+     * H = NZ/2), twx Cx<P>[NX] (exp(-2 pi i n2 k1 / NX) at n2*N1 + k1), ex
+     * P[NX] (E_x(k)/NX) */
 };
 
 size_t scft_step2d_smem(int prec, int nx, int nz);
@@ -173,7 +185,8 @@ cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, in
                                int configure);
 
 /* Internal hooks of scft_ctx.cu for the allocation-free propagator entry point. */
-int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st);
+int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st,
+                  const InstOps **ops0);
 int scft_ctx_run_chain(scft_ctx *c, const ChainDesc *dev_desc, int len);
 void scft_set_error(const char *msg);
 

@@ -45,7 +45,8 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
     long m = 0, sm = 0;
     double ds = 0.0;
     cudaStream_t st = nullptr;
-    scft_ctx_info(ctx, &dev, &prec, &m, &sm, &ds, &st);
+    const InstOps *ops = nullptr;
+    scft_ctx_info(ctx, &dev, &prec, &m, &sm, &ds, &st, &ops);
     if (dev < 0 || dev >= SCFT_STATIC_MAX_DEVICES) return SCFT_ERR_PARAM;
     const size_t psize = prec == SCFT_PREC_FP64 ? 8 : 4;
     const size_t slices = (size_t)steps + 1;
@@ -94,6 +95,7 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
     cd.b1 = bz;
     cd.seg_end = steps + 1;
     cd.len = steps + 1;
+    cd.ops = ops;
     e = cudaMemcpyAsync(desc, &cd, sizeof(cd), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(wd, w, sizeof(double) * m, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(qd, q0, sizeof(double) * m, cudaMemcpyHostToDevice, st);

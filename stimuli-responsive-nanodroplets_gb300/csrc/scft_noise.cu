@@ -63,7 +63,7 @@ __global__ void k_rng_count(NoiseArgs n)
 {
     const int b = blockIdx.y;
     const long chunk = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (chunk >= n.nchunks) return;
+    if (chunk >= n.nchunks || n.state[b].done) return;
     unsigned long long x = jump_to_chunk(n.state_in[b], (unsigned long long)chunk);
     int cnt = 0;
     double x1, w;
@@ -78,6 +78,7 @@ __global__ void k_rng_scan(NoiseArgs n)
     __shared__ long warp_tot[32];
     __shared__ long carry;
     const int b = blockIdx.x;
+    if (n.state[b].done) return; /* uniform over the CTA */
     const int *cnt = n.counts + (long)b * n.nchunks;
     long *pre = n.prefix + (long)b * n.nchunks;
     if (threadIdx.x == 0) carry = 0;
@@ -118,7 +119,7 @@ __global__ void k_rng_emit(NoiseArgs n)
 {
     const int b = blockIdx.y;
     const long chunk = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (chunk >= n.nchunks) return;
+    if (chunk >= n.nchunks || n.state[b].done) return;
     const InstParams &ip = n.params[b];
     const unsigned long iter = n.state[b].iter;
     const double mf = iter > (unsigned long)ip.relaxation ? 0.0 : 1.0;
@@ -155,7 +156,7 @@ __global__ void k_rng_snapshot(NoiseArgs n)
 __global__ void k_rng_check(NoiseArgs n)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < n.B) {
+    if (b < n.B && !n.state[b].done) {
         const long G = (long)n.params[b].n_active * n.m;
         if (n.total[b] < G) n.state[b].status = SCFT_ERR_STATE; /* not enough attempts: never expected */
     }

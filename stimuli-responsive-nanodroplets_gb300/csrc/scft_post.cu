@@ -47,15 +47,19 @@ __global__ void k_iter_begin(PostArgs a)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < a.B) {
-        a.state[b].iter += 1; /* iIter++ (SCFT.c:1090) */
-        a.state[b].status = SCFT_OK;
+        a.state[b].tick += 1;
+        if (a.state[b].done == 2) a.state[b].done = 1; /* converged in the previous iteration */
+        if (!a.state[b].done) {
+            a.state[b].iter += 1; /* iIter++ (SCFT.c:1090) */
+            a.state[b].status = SCFT_OK;
+        }
     }
 }
 
 __global__ void k_iter_start_mark(PostArgs a)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < a.B) a.state[b].iter0 = a.state[b].iter;
+    if (b < a.B) a.state[b].tick = 0;
 }
 
 /* b = exp(DS * (-w/2)) for the fields chains use (SCFT.c:2344), and the initial
@@ -65,6 +69,7 @@ template <typename P>
 __global__ void k_boltz_init(PostArgs a)
 {
     const int b = blockIdx.y;
+    if (a.state[b].done) return;
     const InstParams &ip = a.params[b];
     const unsigned long iter = a.state[b].iter;
     const bool seed_on = ip.enable_seed && iter <= (unsigned long)ip.seed_steps;
@@ -99,8 +104,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_q_partial(PostArgs a)
 {
     __shared__ double sh[32];
     const int sp = blockIdx.y, b = blockIdx.z;
-    const SpeciesDesc sd = a.species[sp];
-    if (!sd.present) return;
+    const SpeciesDesc sd = a.species[b * SCFT_NSPECIES + sp];
+    if (!sd.present || a.state[b].done) return;
     const ChainDesc &cd = a.chains[b * a.nchains + sd.q_chain];
     const P *q = reinterpret_cast<const P *>(cd.q) + (long)(sd.len - 1) * a.sm;
     double v[1] = {0.0};
@@ -113,8 +118,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_q_partial(PostArgs a)
 __global__ void k_q_final(PostArgs a, int nparts)
 {
     const int sp = blockIdx.x, b = blockIdx.y;
-    if (threadIdx.x != 0) return;
-    const SpeciesDesc sd = a.species[sp];
+    if (threadIdx.x != 0 || a.state[b].done) return;
+    const SpeciesDesc sd = a.species[b * SCFT_NSPECIES + sp];
     double q = 0.0;
     if (sd.present) {
         const double *p = a.partial + ((long)b * SCFT_NSPECIES + sp) * nparts;
@@ -193,7 +198,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
     constexpr int V = sizeof(P) == 4 ? 4 : 2;
     using Acc = typename AccOf<P>::T;
     const int blk = blockIdx.y, b = blockIdx.z;
-    const BlockDesc bd = a.blocks[blk];
+    if (a.state[b].done) return;
+    const BlockDesc bd = a.blocks[b * a.nblocks + blk];
     const P *qf = reinterpret_cast<const P *>(a.chains[b * a.nchains + bd.chain_f].q);
     const P *qb = reinterpret_cast<const P *>(a.chains[b * a.nchains + bd.chain_b].q);
     double *out = a.raw + ((long)b * a.nblocks + blk) * a.sm;
@@ -274,11 +280,12 @@ __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
     __shared__ int actf[SCFT_NFIELDS], p0[SCFT_NFIELDS], p1[SCFT_NFIELDS];
     __shared__ int s_na;
     const int b = blockIdx.y;
+    if (a.state[b].done) return;
     const InstParams &ip = a.params[b];
     const InstState &st = a.state[b];
     const double mf = (st.iter > (unsigned long)ip.relaxation) ? 0.0 : 1.0; /* SCFT.c:1515-1522 */
     if (threadIdx.x < a.nblocks) {
-        const BlockDesc bd = a.blocks[threadIdx.x];
+        const BlockDesc bd = a.blocks[b * a.nblocks + threadIdx.x];
         const double ds_eff = 1.0 / (bd.len - 1);
         /* frac * ((raw / 3) * (DS_EFF / Q)) as one factor: the FP64 divisions
          * would otherwise dominate this kernel's FP64 pipe time */
@@ -426,6 +433,13 @@ __global__ void k_finalize(PostArgs a, int nparts)
 {
     const int b = blockIdx.x;
     __shared__ double sh[3 * 32];
+    InstState &st = a.state[b];
+    const long slot = (long)st.tick - 1;
+    if (st.done) {
+        /* frozen: repeat the converging iteration's record */
+        if (threadIdx.x == 0 && slot >= 0 && slot < a.hist_cap) a.hist[slot * a.B + b] = a.last[b];
+        return;
+    }
     double v[3] = {0.0, 0.0, 0.0};
     /* fixed assignment of partials to threads keeps the order deterministic */
     for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
@@ -437,7 +451,6 @@ __global__ void k_finalize(PostArgs a, int nparts)
     block_sum<3>(v, sh);
     if (threadIdx.x != 0) return;
     const InstParams &ip = a.params[b];
-    InstState &st = a.state[b];
     const double dvol = (double)a.m;
     double H = v[0] / dvol;
     double frac = 0.0;
@@ -447,7 +460,7 @@ __global__ void k_finalize(PostArgs a, int nparts)
         const double q = st.q[sp];
         rec.q[sp] = q;
         rec.mu[sp] = 0.0;
-        if (!a.species[sp].present) continue;
+        if (!a.species[b * SCFT_NSPECIES + sp].present) continue;
         const double qm = q * q;
         rec.mu[sp] = (qm == 0.0) ? 0.0 : -log(qm) / 2.0;
         frac += ip.lnq_coef[sp] * log(q);
@@ -464,8 +477,12 @@ __global__ void k_finalize(PostArgs a, int nparts)
     rec.rms = rms;
     rec.mf = (st.iter > (unsigned long)ip.relaxation) ? 0.0 : 1.0;
     rec.status = st.status;
-    rec.pad = 0;
-    const long slot = (long)(st.iter - st.iter0 - 1);
+    rec.converged = 0;
+    if (st.stop_rms > 0.0 && st.status == SCFT_OK && rms < st.stop_rms) {
+        st.done = 2; /* frozen from the next iteration on; this one still ends with the p shift */
+        rec.converged = 1;
+    }
+    a.last[b] = rec;
     if (slot >= 0 && slot < a.hist_cap) a.hist[slot * a.B + b] = rec;
 }
 
@@ -473,6 +490,7 @@ __global__ void k_finalize(PostArgs a, int nparts)
 __global__ void k_p_shift(PostArgs a)
 {
     const int b = blockIdx.y;
+    if (a.state[b].done == 1) return;
     const double pavg = a.state[b].p_avg;
     double *p = a.w + ((long)b * 14 + 13) * a.sm;
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < a.m; idx += (long)gridDim.x * blockDim.x)

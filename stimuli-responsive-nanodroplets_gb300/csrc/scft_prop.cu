@@ -146,6 +146,7 @@ template <typename P>
 __global__ void __launch_bounds__(256) k_pass_fft(AxisGeom g, PassArgs a)
 {
     const ChainDesc cd = a.chains[blockIdx.y];
+    if (a.state && a.state[cd.instance].done) return; /* uniform over the CTA */
     if (a.s >= cd.len - 1) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n;
@@ -161,9 +162,11 @@ __global__ void __launch_bounds__(256) k_pass_fft(AxisGeom g, PassArgs a)
     P *dst = a.last ? reinterpret_cast<P *>(cd.q) + (long)(a.s + 1) * a.sstride : reinterpret_cast<P *>(cd.tmp);
     const P *bz = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
 
+    const Cx<P> *gtw = reinterpret_cast<const Cx<P> *>(cd.ops->tw[a.axis]);
+    const P *gspec = reinterpret_cast<const P *>(cd.ops->spec[a.axis]);
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        tw[t] = reinterpret_cast<const Cx<P> *>(a.tw)[t];
-        spec[t] = reinterpret_cast<const P *>(a.spec)[t];
+        tw[t] = gtw[t];
+        spec[t] = gspec[t];
     }
     const long L0 = (long)blockIdx.x * a.tile;
     const int total = a.tile * n;
@@ -224,6 +227,7 @@ template <typename P>
 __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
 {
     const ChainDesc cd = a.chains[blockIdx.y];
+    if (a.state && a.state[cd.instance].done) return; /* uniform over the CTA */
     if (a.s >= cd.len - 1) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, h = a.h;
@@ -237,8 +241,8 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
                            : reinterpret_cast<const P *>(cd.tmp);
     P *dst = a.last ? reinterpret_cast<P *>(cd.q) + (long)(a.s + 1) * a.sstride : reinterpret_cast<P *>(cd.tmp);
     const P *bz = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
-    const P *gA = reinterpret_cast<const P *>(a.kA);
-    const P *gB = reinterpret_cast<const P *>(a.kB);
+    const P *gA = reinterpret_cast<const P *>(cd.ops->kA[a.axis]);
+    const P *gB = reinterpret_cast<const P *>(cd.ops->kB[a.axis]);
     for (int e = threadIdx.x; e < h * h; e += blockDim.x) {
         kA[e] = gA[e];
         if (a.even) kB[e] = gB[e];

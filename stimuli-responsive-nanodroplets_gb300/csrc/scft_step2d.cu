@@ -285,6 +285,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     using T2 = typename V2<P>::T;
 
     const ChainDesc cd = a.chains[a.order ? a.order[blockIdx.x] : blockIdx.x];
+    if (a.state && a.state[cd.instance].done) return; /* uniform over the CTA */
     const int s_end = a.s_end < cd.len - 1 ? a.s_end : cd.len - 1;
     if (a.s >= s_end) return;
 
@@ -303,14 +304,14 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     /* operators and tables, once per chain (16-byte asynchronous copies) */
     {
         constexpr int VP = 16 / sizeof(P);
-        const P *gA = reinterpret_cast<const P *>(a.kz);
+        const P *gA = reinterpret_cast<const P *>(cd.ops->kz);
         for (int e = tid; e < H * H / VP; e += NX) {
             cp_async16(KA + e * VP, gA + e * VP);
             cp_async16(KB + e * VP, gA + H * H + e * VP);
         }
-        const P *gT = reinterpret_cast<const P *>(a.twx);
+        const P *gT = reinterpret_cast<const P *>(cd.ops->twx);
         for (int e = tid; e < 2 * NX / VP; e += NX) cp_async16(reinterpret_cast<P *>(TW) + e * VP, gT + e * VP);
-        const P *gE = reinterpret_cast<const P *>(a.ex);
+        const P *gE = reinterpret_cast<const P *>(cd.ops->ex);
         for (int e = tid; e < NX / VP; e += NX) cp_async16(EX + e * VP, gE + e * VP);
     }
     /* load q_s into the padded rows with asynchronous 2-element copies: every

@@ -63,15 +63,17 @@ class IterOut:
     mu: np.ndarray
     q: np.ndarray
     status: int
+    converged: int = 0
 
     @classmethod
     def from_c(cls, r: L.CIterOut) -> "IterOut":
         return cls(int(r.iter), float(r.free_energy), float(r.rms), float(r.mf), np.array(r.mu[:]), np.array(r.q[:]),
-                   int(r.status))
+                   int(r.status), int(r.converged))
 
     def to_c(self) -> L.CIterOut:
         r = L.CIterOut()
         r.iter, r.free_energy, r.rms, r.mf, r.status = self.iter, self.free_energy, self.rms, self.mf, self.status
+        r.converged = self.converged
         for k in range(L.NSP):
             r.mu[k] = self.mu[k]
             r.q[k] = self.q[k]
@@ -173,6 +175,36 @@ class Solver:
             noise = np.ascontiguousarray(noise, dtype=np.float64)
             nd = _dp(noise)
         L.check(L.lib().scft_iterate(self._h, n, nd, outs), "scft_iterate")
+        return [[IterOut.from_c(outs[k * self.B + b]) for b in range(self.B)] for k in range(n)]
+
+    def set_surface(self, instance: int, surface: Surface):
+        """Give a slot new parameters (same grid and composition; NS within the slot's capacity)."""
+        cs = L.CSurface.from_surface(surface)
+        L.check(L.lib().scft_set_surface(self._h, instance, C.byref(cs)), "scft_set_surface")
+        self.surfaces[instance] = surface
+        d = L.CDerived()
+        L.check(L.lib().scft_ctx_derived(self._h, instance, C.byref(d)), "scft_ctx_derived")
+        self.derived[instance] = Derived(d, 0)
+
+    def freeze(self, instance: int):
+        """Idle a slot: later iterations skip it until set_iteration re-arms it."""
+        L.check(L.lib().scft_freeze(self._h, instance), "scft_freeze")
+
+    def set_stop(self, rms_tol: float, instance: Optional[int] = None):
+        """Freeze an instance (every instance if None) once RMS(phi_tot-1) < rms_tol."""
+        for b in (range(self.B) if instance is None else [instance]):
+            L.check(L.lib().scft_set_stop(self._h, b, float(rms_tol)), "scft_set_stop")
+
+    def iterate_async(self, n: int):
+        """Enqueue n <= 256 iterations (device noise or no noise) without waiting."""
+        L.check(L.lib().scft_iterate_async(self._h, int(n)), "scft_iterate_async")
+        self._pending = int(n)
+
+    def iterate_wait(self) -> List[List[IterOut]]:
+        n = getattr(self, "_pending", 0)
+        outs = (L.CIterOut * max(1, n * self.B))()
+        L.check(L.lib().scft_iterate_wait(self._h, outs), "scft_iterate_wait")
+        self._pending = 0
         return [[IterOut.from_c(outs[k * self.B + b]) for b in range(self.B)] for k in range(n)]
 
     def get_fields(self, instance: int = 0) -> np.ndarray:
