@@ -124,3 +124,66 @@ def sweep_surfaces(n: int = 16, seed: int = 3, sizes=((64, 64), (96, 64), (128, 
             ns = int(rng.integers(ns_range[0], ns_range[1] + 1))
             out.append(film2d(nx=nx, nz=nz, ns=ns, chi_ab=chi_ab, chi_ac=chi_ac))
     return out
+
+
+# ------------------------------------------------------- phase-diagram planes
+# The phase diagram is a (chi_AB N, chi_AC N) grid repeated over three planes,
+# one per starting contact angle; a plane fixes the other interactions. Here a
+# plane sets the brush-S1 interactions of the thin film (S1 neutral, S1
+# solvent-philic, S1 copolymer-philic) and chi_BC N of the 3D bulk blend.
+PLANES = (
+    {"name": "P0", "S1C": 5.0, "S1AB": 10.0, "BC": 35.0},   # near 90 degrees
+    {"name": "P1", "S1C": 0.0, "S1AB": 20.0, "BC": 25.0},   # near dewetted
+    {"name": "P2", "S1C": 20.0, "S1AB": 0.0, "BC": 45.0},   # near wetted
+)
+
+
+def chi_axes(n: int = 24, ab=(10.0, 30.0), ac=(20.0, 60.0)):
+    """The (chi_AB N, chi_AC N) grid values of an n x n plane."""
+    return (np.array([ab[0] + (ab[1] - ab[0]) * i / max(n - 1, 1) for i in range(n)]),
+            np.array([ac[0] + (ac[1] - ac[0]) * j / max(n - 1, 1) for j in range(n)]))
+
+
+def film_point(chi_ab: float, chi_ac: float, plane: dict, nx: int = 192, nz: int = 96, ns: int = 100) -> Surface:
+    """Thin-film droplet chemistry at one phase-diagram point of a plane."""
+    s = film2d(nx=nx, nz=nz, ns=ns, chi_ab=chi_ab, chi_ac=chi_ac)
+    s.set_chi("S1", "C", plane["S1C"]).set_chi("S1", "A", plane["S1AB"]).set_chi("S1", "B", plane["S1AB"])
+    return s
+
+
+def bulk3d_point(chi_ab: float, chi_ac: float, plane: dict, n: int = 64, ns: int = 100) -> Surface:
+    """3D bulk (MASK 0) AB diblock f = 0.5 at VOL 0.4 in homopolymer C solvent at
+    0.6; LX = LY = LZ = 8 R_g (64^3 at DR_TARGET 0.125), G1 = 0.05, noise off."""
+    L = n * 0.125
+    s = Surface(LX=L, LY=L, LZ=L, ITER=5000, D_WRT=5000, RELAXATION=0, D_WRT_ENERGIES=1, DT_NOISE=0.0, MASK=0,
+                ENABLE_SEED=0, NS=ns, DR_TARGET=0.125, G1=0.05)
+    s.VOL_DBK = [0.4, 0.0, 0.0, 0.0]
+    s.F_INPUT_DBK = [0.5, 0.5, 0.5, 0.5]
+    s.VOL_HOMO = [0.0, 0.0, 0.6] + [0.0] * 7
+    s.set_chi("A", "B", chi_ab).set_chi("A", "C", chi_ac).set_chi("B", "C", plane["BC"])
+    return s
+
+
+def seed_fields(s: Surface, kind: str, seed: int, amp: float = 0.05) -> np.ndarray:
+    """Synthetic first-pass seeds: "lamellar" (w_A - w_B ~ cos along x),
+    "cylinder" (cos along x times cos along z), "disordered" (noise only), inside
+    the droplet of a film (MASK 1) or everywhere in a bulk box; every field gets
+    uniform[-amp, amp] noise from the seed."""
+    nx, ny, nz = s.grid()
+    i, j, k = idx_coords(nx, ny, nz)
+    if s.MASK:
+        w = droplet_fields(s, seed=seed, radius=min(6.0, 0.3 * s.LX, 0.6 * s.LZ), amp=amp)
+    else:
+        w = uniform_fields((nx, ny, nz), seed=seed, amp=amp, fields=(0, 1, 2))
+    periods = 4.0
+    if kind == "lamellar":
+        pat = np.cos(2.0 * np.pi * periods * i / nx)
+    elif kind == "cylinder":
+        pat = np.cos(2.0 * np.pi * periods * i / nx) * np.cos(2.0 * np.pi * 2.0 * k / nz)
+    elif kind == "disordered":
+        pat = np.zeros(nx * ny * nz)
+    else:
+        raise ValueError(f"unknown seed kind {kind!r}")
+    w[0] += 1.5 * pat
+    w[1] -= 1.5 * pat
+    return w
