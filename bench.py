@@ -43,6 +43,7 @@ sys.path.insert(0, str(ROOT))
 PKG = "stimuli-responsive-nanodroplets_gb300"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC = ROOT / "profiles" / "traffic.json"
+METRIC = "SCFT iters/s & solves/hr, fused FP32 vs plain FP64 on 1 GB300; p50/p99 solve latency"
 
 
 def dist_env():
@@ -217,6 +218,103 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
     return res
 
 
+def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, fp64_iters: int, device: int, sync):
+    """The 2D droplet sweep (n x n chi points, uneven grids and NS) run to
+    RMS < rms_tol in the precision form: converged solves/hour. The plain FP64
+    form runs the same batch for fp64_iters iterations; its solves/hour is its
+    instance-iteration rate over the iterations the precision form needed per
+    solve (same start, same stop rule)."""
+    sw = importlib.import_module(f"{PKG}.sweep")
+    surfaces = srn.configs.sweep_surfaces(n, seed=3, sizes=sw.SWEEP_SIZES, ns_range=(64, 128))
+    inputs = sw.sweep_inputs(surfaces)
+    sync()
+    with sw.make_batch(surfaces, inputs, "fp32", rms_tol) as b:
+        t0 = time.perf_counter()
+        res = b.run(max_iter, chunk=200)
+        sync()
+        wall32 = time.perf_counter() - t0
+        groups = b.groups
+    its = np.array([r.iterations for r in res])
+    conv = int(sum(r.converged for r in res))
+    out = {"instances": len(res), "groups": groups, "rms_tol": rms_tol, "max_iter": max_iter,
+           "fp32": {"converged": conv, "wall_s": wall32, "solves_per_hour": conv * 3600.0 / wall32,
+                    "iterations_median": float(np.median(its)), "iterations_max": int(its.max()),
+                    "instance_iterations_per_s": float(its.sum()) / wall32}}
+    if fp64_iters > 0:
+        with sw.make_batch(surfaces, inputs, "fp64", rms_tol) as b:
+            b.run(2, chunk=2)  # graph capture and first touch outside the timed region
+            sync()
+            t0 = time.perf_counter()
+            r64 = b.run(fp64_iters, chunk=min(fp64_iters, 200))
+            sync()
+            wall64 = time.perf_counter() - t0
+        done64 = sum(r.iterations for r in r64)
+        rate64 = done64 / wall64
+        per_solve = float(its.mean())
+        out["fp64_plain"] = {"instance_iterations_per_s": rate64, "iterations_timed": fp64_iters,
+                             "solves_per_hour": rate64 * 3600.0 / per_solve,
+                             "method": "rate over the first iterations x mean iterations per solve of the "
+                                       "precision form"}
+        out["solves_per_hour_ratio_fp32_over_fp64"] = out["fp32"]["solves_per_hour"] / out["fp64_plain"][
+            "solves_per_hour"]
+    return out
+
+
+def measure_serving(srn, n_requests: int, rate_hz: float, rms_tol: float, max_iter: int, device: int):
+    """Poisson stream of phase-diagram solve requests: 70% 2D 192x96 thin film
+    (one in five of those in the plain FP64 form), 30% 3D 64^3 bulk blend, NS =
+    100, first-pass synthetic seeds (lamellar / cylinder / disordered); slots
+    from a device-memory budget; p50/p99 time to converged."""
+    serve = importlib.import_module(f"{PKG}.serve")
+    cfg = srn.configs
+    rng = np.random.default_rng(7)
+    chi_ab, chi_ac = cfg.chi_axes(24)
+    ft = cfg.film_point(20.0, 40.0, cfg.PLANES[0], ns=100)
+    bt = cfg.bulk3d_point(20.0, 40.0, cfg.PLANES[0], ns=100)
+    kinds = ("lamellar", "cylinder", "disordered")
+    reqs = []
+    t = 0.0
+    for r in range(n_requests):
+        t += float(rng.exponential(1.0 / rate_hz))
+        plane = cfg.PLANES[int(rng.integers(3))]
+        i, j = int(rng.integers(24)), int(rng.integers(24))
+        kind = kinds[int(rng.integers(3))]
+        if rng.random() < 0.7:
+            s = cfg.film_point(float(chi_ab[i]), float(chi_ac[j]), plane, ns=100)
+            prec = "fp64" if rng.random() < 0.2 else "fp32"
+            reqs.append(serve.Request(rid=r, cls="film2d", surface=s, w14=cfg.seed_fields(s, kind, seed=r),
+                                      mask3=cfg.substrate_mask(s), precision=prec, arrival=t,
+                                      key=(plane["name"], i, j), seed=(r, 5, 7)))
+        else:
+            s = cfg.bulk3d_point(float(chi_ab[i]), float(chi_ac[j]), plane, ns=100)
+            reqs.append(serve.Request(rid=r, cls="bulk3d", surface=s, w14=cfg.seed_fields(s, kind, seed=r),
+                                      precision="fp32", arrival=t, key=(plane["name"], i, j), seed=(r, 5, 7)))
+    budget = 24 << 30  # device memory the pools may hold
+    slots = {("film2d", "fp32"): serve.slots_for_budget(ft, "fp32", budget // 2, max_slots=64),
+             ("film2d", "fp64"): serve.slots_for_budget(ft, "fp64", budget // 6, max_slots=16),
+             ("bulk3d", "fp32"): serve.slots_for_budget(bt, "fp32", budget // 3, max_slots=16)}
+    tmpl = {"film2d": ft, "bulk3d": bt}
+    chunks = {"film2d": 100, "bulk3d": 10}  # about a quarter second of device time per round
+    pools = {k: serve.Pool(k[0], tmpl[k[0]], v, k[1], chunk=chunks[k[0]]) for k, v in slots.items()}
+    server = serve.Server(pools, rms_tol=rms_tol, max_iter=max_iter, chunk=50)
+    t0 = time.perf_counter()
+    done = server.run(reqs)
+    wall = time.perf_counter() - t0
+    server.close()
+    st = serve.latency_stats(done, wall)
+    by = {}
+    for k in slots:
+        cs = [c for c in done if (c.cls, c.precision) == k]
+        if cs:
+            lat = np.array([c.latency for c in cs])
+            by[f"{k[0]}/{k[1]}"] = {"requests": len(cs), "converged": int(sum(c.converged for c in cs)),
+                                    "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                                    "iterations_median": float(np.median([c.iterations for c in cs]))}
+    st.update({"rate_hz": rate_hz, "rms_tol": rms_tol, "max_iter": max_iter, "wall_s": wall,
+               "slots": {f"{k[0]}/{k[1]}": v for k, v in slots.items()}, "by_class": by})
+    return st
+
+
 def cpu_sample(surfaces, threads: int, iters: int):
     """The CPU restatement of SCFT.c, one instance per thread (ctypes drops the GIL)."""
     srn = importlib.import_module(PKG)
@@ -266,7 +364,7 @@ def run_reference(args, rank, world):
         t_all += wall
     value = threads * steps / t_all
     line = {
-        "impl": "reference", "metric": "SCFT iterations/s", "value": value, "unit": "instance-iterations/s",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "instance-iterations/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded droplet fields)",
@@ -305,6 +403,14 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--sweep-n", type=int, default=16, help="n x n chi points of the droplet sweep (0: skip)")
+    ap.add_argument("--sweep-tol", type=float, default=1e-4)
+    ap.add_argument("--sweep-max-iter", type=int, default=5000)
+    ap.add_argument("--sweep-fp64-iters", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=40, help="requests of the serving stream (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="mean arrivals per second")
+    ap.add_argument("--serve-tol", type=float, default=1e-3)
+    ap.add_argument("--serve-max-iter", type=int, default=3000)
     ap.add_argument("--profile-case", action="store_true",
                     help="one iteration of one form only (for ncu captures); prints no bench line")
     args = ap.parse_args()
@@ -362,7 +468,7 @@ def main():
     if TRAFFIC.exists():
         traffic = json.loads(TRAFFIC.read_text()).get("fp32", {}).get("traffic_bytes_per_launch")
     line = {
-        "metric": "SCFT iterations/s", "value": value, "unit": "instance-iterations/s", "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": "instance-iterations/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 propagators, f64 densities/Q/free energy/update",
         "data": "synthetic (seeded half-disk droplet fields, chi sweep)",
@@ -383,6 +489,12 @@ def main():
                    "contour_steps_per_instance_iteration": f32["contour_steps_per_instance_iteration"],
                    "device_bytes_fp32": f32["device_bytes"]},
     }
+    if args.sweep_n > 0:
+        line["sweep"] = measure_sweep(srn, args.sweep_n, args.sweep_tol, args.sweep_max_iter, args.sweep_fp64_iters,
+                                      local, sync)
+    if args.serve_requests > 0:
+        line["serving"] = measure_serving(srn, args.serve_requests, args.serve_rate, args.serve_tol,
+                                          args.serve_max_iter, local)
     if rank == 0 and not args.no_cpu:
         threads = args.cpu_threads or os.cpu_count() or 1
         rate, wall = cpu_sample(surfaces, threads, args.cpu_iters)

@@ -108,7 +108,10 @@ typedef struct scft_options {
     int n_instances; /* instances in this context (batching form); 1 for a single solve */
     int kernel_path; /* 0: fused single-launch contour step where the shape has one, else per-axis
                         passes; 1: per-axis passes only */
-    int reserved[2];
+    int autotune;    /* 1 (default): time the per-axis pass tile candidates on the context's own
+                        chains at creation and keep the fastest (cached per shape and batch size);
+                        0: heuristic tiles. Every candidate gives bit-identical results. */
+    int reserved;
 } scft_options;
 
 void scft_options_default(scft_options *o);
@@ -183,6 +186,9 @@ int scft_iterate(scft_ctx *ctx, int n, const double *noise, scft_iter_out *out);
 #define SCFT_HIST_CAP 256
 int scft_iterate_async(scft_ctx *ctx, int n);
 int scft_iterate_wait(scft_ctx *ctx, scft_iter_out *out);
+/* 1 when the enqueued iterations have finished (or none are enqueued), 0 while
+ * they run, a negative status on a device error. Never blocks. */
+int scft_iterate_ready(scft_ctx *ctx);
 
 /* Batching form over uneven grid sizes (no counterpart in the reference, which
  * runs one instance per process). A batch groups n surfaces by grid, MASK,

@@ -85,7 +85,7 @@ class CDerived(C.Structure):
 
 class COptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("noise_mode", C.c_int), ("use_graph", C.c_int),
-                ("n_instances", C.c_int), ("kernel_path", C.c_int), ("reserved", C.c_int * 2)]
+                ("n_instances", C.c_int), ("kernel_path", C.c_int), ("autotune", C.c_int), ("reserved", C.c_int)]
 
 
 class CIterOut(C.Structure):
@@ -135,6 +135,7 @@ def lib() -> C.CDLL:
         "scft_set_surface": (I, [VP, I, P(CSurface)]),
         "scft_iterate_async": (I, [VP, I]),
         "scft_iterate_wait": (I, [VP, P(CIterOut)]),
+        "scft_iterate_ready": (I, [VP]),
         "scft_batch_create": (I, [P(CSurface), I, P(COptions), P(VP)]),
         "scft_batch_destroy": (I, [VP]),
         "scft_batch_groups": (I, [VP]),

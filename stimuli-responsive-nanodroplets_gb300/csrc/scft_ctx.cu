@@ -20,6 +20,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "scft_internal.h"
@@ -107,6 +110,7 @@ struct scft_ctx {
     scft_iter_out *hist_host = nullptr; /* pinned */
     int hist_cap = 0;
     int pending = 0; /* iterations enqueued and not yet collected */
+    cudaEvent_t chunk_done = nullptr; /* recorded after the records copy of the enqueued chunk */
     int nparts = 0;
     size_t device_bytes = 0;
     std::vector<void *> allocs;
@@ -151,6 +155,7 @@ extern "C" void scft_options_default(scft_options *o)
     o->noise_mode = SCFT_NOISE_HOST;
     o->use_graph = 0;
     o->n_instances = 1;
+    o->autotune = 1;
 }
 
 /* ------------------------------------------------------- shape helpers */
@@ -482,6 +487,94 @@ static int build_axes(scft_ctx *c)
     return SCFT_OK;
 }
 
+/* ------------------------------------------------------------ autotuner */
+/* Tiles (lines per CTA) of the per-axis passes, timed on the context's own
+ * chains: every candidate that divides the axis' line layout and fits shared
+ * memory runs a few contour-step passes, and the fastest is kept. Only even
+ * tiles are candidates for the FFT passes, so the pairing of real lines into
+ * complex ones (2q, 2q+1) and with it every rounding is the same for every
+ * candidate: tuning never changes results. The radix order is not tuned for
+ * the same reason (it would change the rounding). Choices are cached per
+ * precision, axis geometry and number of chains. */
+static std::mutex g_tune_mu;
+static std::map<std::string, int> g_tune_cache;
+
+static int autotune_axes(scft_ctx *c)
+{
+    if (c->axes.empty()) return SCFT_OK;
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    const int npass = (int)c->axes.size();
+    const int total = c->B * c->nchains;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int rc = SCFT_OK;
+    for (int ai = 0; ai < npass && rc == SCFT_OK; ++ai) {
+        Axis &A = c->axes[ai];
+        const long lines = c->m / A.g.n;
+        const long divisor = A.src == 2 ? lines : A.g.inner;
+        char key[160];
+        snprintf(key, sizeof(key), "%d|%d,%d,%d,%d,%d|%d|%d", c->psize, A.g.n, A.g.ls, A.g.inner, A.g.outer,
+                 A.g.dirichlet, total, ai == 0 ? 1 : (ai == npass - 1 ? 2 : 0));
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                A.tile = it->second;
+                A.ntiles = (int)(lines / A.tile);
+                continue;
+            }
+        }
+        std::vector<int> cand;
+        for (int t = A.g.dirichlet ? 1 : 2; t <= 64; t *= 2)
+            if (divisor % t == 0 && lines / t >= 1 && scft_pass_smem_bytes(A.g, t, A.h, c->psize) <= (size_t)optin)
+                cand.push_back(t);
+        if (cand.size() > 1) {
+            float best_ms = 1e30f;
+            int best = A.tile;
+            for (int t : cand) {
+                PassArgs pa;
+                memset(&pa, 0, sizeof(pa));
+                pa.chains = c->chains;
+                pa.nchains = total;
+                pa.s = 0;
+                pa.first = ai == 0;
+                pa.last = ai == npass - 1;
+                pa.tile = t;
+                pa.sstride = c->sm;
+                pa.axis = ai;
+                pa.h = A.h;
+                pa.even = A.even;
+                const int nt = (int)(lines / t);
+                cudaError_t e = scft_launch_pass(c->opt.precision, A.g, pa, nt, c->stream); /* warm-up */
+                if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+                for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = scft_launch_pass(c->opt.precision, A.g, pa, nt, c->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess) {
+                    set_err("autotune: %s", cudaGetErrorString(e));
+                    rc = SCFT_ERR_CUDA;
+                    break;
+                }
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                }
+            }
+            A.tile = best;
+            A.ntiles = (int)(lines / A.tile);
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = A.tile;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
 /* Instances of one context share the grid, the MASK setting and the active
  * field set (the noise layout); the species composition is compared after the
  * chains are built. */
@@ -591,6 +684,7 @@ extern "C" int scft_ctx_destroy(scft_ctx *c)
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->graph) cudaGraphDestroy(c->graph);
     for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+    if (c->chunk_done) cudaEventDestroy(c->chunk_done);
     for (void *p : c->allocs) cudaFree(p);
     if (c->hist_host) cudaFreeHost(c->hist_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -799,6 +893,10 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         }
     }
 #undef ALLOC
+    if (opt.autotune && !c->fused2d && (rc = autotune_axes(c))) {
+        scft_ctx_destroy(c);
+        return rc;
+    }
     {
         /* longest chains first, so the persistent launch ends with short ones */
         std::vector<int> ord((size_t)B * c->nchains);
@@ -1173,6 +1271,8 @@ static int enqueue_chunk(scft_ctx *c, int chunk, const double *noise)
     if (c->timing) CK(cudaEventRecord(c->ev[1], c->stream));
     CK(cudaMemcpyAsync(c->hist_host, c->hist, sizeof(scft_iter_out) * chunk * c->B, cudaMemcpyDeviceToHost,
                        c->stream));
+    if (!c->chunk_done) CK(cudaEventCreateWithFlags(&c->chunk_done, cudaEventDisableTiming));
+    CK(cudaEventRecord(c->chunk_done, c->stream));
     c->pending = chunk;
     return SCFT_OK;
 }
@@ -1278,6 +1378,18 @@ extern "C" int scft_iterate_async(scft_ctx *c, int n)
         c->pending = 0;
     }
     return rc;
+}
+
+extern "C" int scft_iterate_ready(scft_ctx *c)
+{
+    if (!c) return SCFT_ERR_PARAM;
+    if (!c->pending) return 1;
+    cudaSetDevice(c->device);
+    const cudaError_t e = cudaEventQuery(c->chunk_done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    set_err("scft_iterate_ready: %s", cudaGetErrorString(e));
+    return SCFT_ERR_CUDA;
 }
 
 extern "C" int scft_iterate_wait(scft_ctx *c, scft_iter_out *out)

@@ -163,36 +163,63 @@ int main(void)
     unsigned short saved[3] = {seed[0], seed[1], seed[2]};
     enum { CHUNK = 256 };
     scft_iter_out *recs = malloc(sizeof(scft_iter_out) * CHUNK);
-    if (!recs) die("Error allocating host buffers");
-    while (iter <= (unsigned long)S.iter) { /* SCFT.c:1088: iterations iter+1 .. ITER+1 */
-        /* run up to the next snapshot (or CHUNK iterations) in one call */
-        unsigned long last = iter + 1;
-        while (last < (unsigned long)S.iter + 1 && last - iter < CHUNK && !(fmod((double)last, (double)S.d_wrt) == 0 || last == 1))
-            ++last;
-        int n = (int)(last - iter);
-        if (host_noise) n = 1;
-        for (int k = 0; k < n && host_noise; ++k) {
-            const unsigned long it = iter + 1;
-            const double mf = it > (unsigned long)S.relaxation ? 0.0 : 1.0;
-            const int need = mf * S.dt_noise != 0.0;
-            /* the reference draws its noise every iteration, used or not */
-            scft_noise_fill(seed, &d, need ? noise : NULL);
-            check(scft_iterate(ctx, 1, need ? noise : NULL, recs), "scft_iterate");
+    scft_iter_out *done_recs = malloc(sizeof(scft_iter_out) * CHUNK);
+    if (!recs || !done_recs) die("Error allocating host buffers");
+    /* Output of a finished chunk (its energies lines and, at a snapshot, the
+     * snapshot files) is written while the next chunk runs on the GPU; the
+     * files and their order are those of the synchronous loop. */
+    int done_n = 0, done_snap = 0;
+    unsigned long done_first = 0, done_iter = 0;
+    unsigned short done_saved[3] = {0, 0, 0};
+    while (iter <= (unsigned long)S.iter || done_n > 0 || done_snap) {
+        int n = 0;
+        if (iter <= (unsigned long)S.iter) { /* SCFT.c:1088: iterations iter+1 .. ITER+1 */
+            /* run up to the next snapshot (or CHUNK iterations) in one call */
+            unsigned long last = iter + 1;
+            while (last < (unsigned long)S.iter + 1 && last - iter < CHUNK &&
+                   !(fmod((double)last, (double)S.d_wrt) == 0 || last == 1))
+                ++last;
+            n = (int)(last - iter);
+            if (host_noise) {
+                n = 1;
+                const unsigned long it = iter + 1;
+                const double mf = it > (unsigned long)S.relaxation ? 0.0 : 1.0;
+                const int need = mf * S.dt_noise != 0.0;
+                /* the reference draws its noise every iteration, used or not */
+                scft_noise_fill(seed, &d, need ? noise : NULL);
+                check(scft_iterate(ctx, 1, need ? noise : NULL, recs), "scft_iterate");
+            } else {
+                check(scft_iterate_async(ctx, n), "scft_iterate_async");
+            }
         }
-        if (!host_noise) check(scft_iterate(ctx, n, NULL, recs), "scft_iterate");
-        for (int k = 0; k < n; ++k) {
-            const unsigned long it = iter + 1 + (unsigned long)k;
-            if (fmod((double)it, (double)S.d_wrt_energies) == 0) check(scft_write_energies(NULL, &d, &recs[k]), "energies");
+        /* the previous chunk's output, overlapping the GPU work just enqueued */
+        for (int k = 0; k < done_n; ++k) {
+            const unsigned long it = done_first + (unsigned long)k;
+            if (fmod((double)it, (double)S.d_wrt_energies) == 0)
+                check(scft_write_energies(NULL, &d, &done_recs[k]), "energies");
         }
+        done_n = 0;
+        if (done_snap) {
+            check(scft_write_snapshot(NULL, &d, done_iter, phi13, w14, done_saved), "snapshot");
+            done_snap = 0;
+        }
+        if (n == 0) break;
+        if (!host_noise) check(scft_iterate_wait(ctx, recs), "scft_iterate_wait");
+        memcpy(done_recs, recs, sizeof(scft_iter_out) * (size_t)n);
+        done_n = n;
+        done_first = iter + 1;
         iter += (unsigned long)n;
         if (fmod((double)iter, (double)S.d_wrt) == 0 || iter == 1) {
             if (!host_noise) check(scft_get_rng(ctx, 0, seed), "scft_get_rng");
             check(scft_get_fields(ctx, 0, w14), "scft_get_fields");
             check(scft_get_densities(ctx, 0, phi13, NULL), "scft_get_densities");
-            check(scft_write_snapshot(NULL, &d, iter, phi13, w14, saved), "snapshot");
+            memcpy(done_saved, saved, sizeof(saved));
             memcpy(saved, seed, sizeof(saved));
+            done_iter = iter;
+            done_snap = 1;
         }
     }
+    free(done_recs);
     free(recs);
     scft_ctx_destroy(ctx);
     free(mask3);

@@ -9,7 +9,10 @@ chunk of iterations on every context with busy slots (the contexts' streams
 run side by side), then collects the records: a slot whose instance met the
 RMS tolerance, or ran out of iterations, completes its request and takes the
 next queued one at once (scft_set_surface + scft_set_fields on the freed
-slot; idle slots are frozen and cost nothing on the device).
+slot; idle slots are frozen and cost nothing on the device). Every pool runs
+its own rounds: the loop polls the pools without blocking, collects a pool as
+soon as its chunk has finished and refills and relaunches it at once, so a
+pool of fast 2D solves is never held back by a pool of slower 3D ones.
 
 Per-instance arithmetic does not depend on the other slots (reductions run in
 a fixed order per instance, operator tables depend only on the instance's own
@@ -74,8 +77,9 @@ class Pool:
     NS the pool serves (it fixes the contour slices allocated per slot)."""
 
     def __init__(self, cls: str, template: Surface, slots: int, precision: str, use_graph: bool = True,
-                 solver=None):
+                 solver=None, chunk: Optional[int] = None):
         self.cls, self.precision, self.slots = cls, precision, int(slots)
+        self.chunk = chunk  # iterations per round (None: the server's)
         self.sv = solver if solver is not None else Solver([template] * self.slots, precision=precision,
                                                             use_graph=use_graph, noise="device")
         zero = np.zeros((14, self.sv.M))
@@ -104,11 +108,15 @@ class Pool:
         self.busy[b] = (req, now, 0)
 
     def launch(self, chunk: int) -> bool:
-        if not self.busy:
+        if not self.busy or self.in_flight:
             return False
-        self.sv.iterate_async(chunk)
-        self.in_flight = chunk
+        n = self.chunk or chunk
+        self.sv.iterate_async(n)
+        self.in_flight = n
         return True
+
+    def ready(self) -> bool:
+        return bool(self.in_flight) and self.sv.iterate_ready()
 
     def collect(self, now_fn: Callable[[], float], max_iter: int, keep_fields: bool) -> List[Completion]:
         if not self.in_flight:
@@ -172,20 +180,26 @@ class Server:
         nxt = 0
         out: List[Completion] = []
         while nxt < len(reqs) or any(queues[k] for k in queues) or any(p.busy for p in self.pools.values()):
+            progressed = False
             now = now_fn()
             while nxt < len(reqs) and reqs[nxt].arrival <= now:
                 queues[(reqs[nxt].cls, reqs[nxt].precision)].append(reqs[nxt])
                 nxt += 1
             for k, pool in self.pools.items():
+                if pool.in_flight:
+                    if not pool.ready():
+                        continue
+                    out.extend(pool.collect(now_fn, self.max_iter, self.keep_fields))
+                    progressed = True
                 while queues[k] and pool.free:
                     pool.admit(queues[k].popleft(), now_fn(), self.rms_tol)
-            launched = [p.launch(self.chunk) for p in self.pools.values()]
-            if not any(launched):
-                if nxt < len(reqs):
-                    time.sleep(max(0.0, min(0.01, reqs[nxt].arrival - now_fn())))
-                continue
-            for p in self.pools.values():
-                out.extend(p.collect(now_fn, self.max_iter, self.keep_fields))
+                if pool.launch(self.chunk):
+                    progressed = True
+            if not progressed:
+                busy = any(p.in_flight for p in self.pools.values())
+                wait = 0.0005 if busy else (max(0.0, min(0.01, reqs[nxt].arrival - now_fn())) if nxt < len(reqs)
+                                            else 0.0)
+                time.sleep(wait)
         return out
 
     def close(self):

@@ -98,7 +98,7 @@ class Solver:
     """
 
     def __init__(self, surfaces: Surface | Sequence[Surface], precision: str = "fp64", device: int = 0,
-                 use_graph: bool = False, kernel_path: str = "auto", noise: str = "host"):
+                 use_graph: bool = False, kernel_path: str = "auto", noise: str = "host", autotune: bool = True):
         if isinstance(surfaces, Surface):
             surfaces = [surfaces]
         self.surfaces = list(surfaces)
@@ -112,6 +112,7 @@ class Solver:
         opt.n_instances = self.B
         opt.kernel_path = {"auto": 0, "passes": 1}[kernel_path]
         opt.noise_mode = {"host": L.NOISE_HOST, "device": L.NOISE_DRAND48}[noise]
+        opt.autotune = int(bool(autotune))
         self.noise_mode = noise
         self.precision = precision
         h = C.c_void_p()
@@ -199,6 +200,13 @@ class Solver:
         """Enqueue n <= 256 iterations (device noise or no noise) without waiting."""
         L.check(L.lib().scft_iterate_async(self._h, int(n)), "scft_iterate_async")
         self._pending = int(n)
+
+    def iterate_ready(self) -> bool:
+        """True once the enqueued iterations have finished (never blocks)."""
+        r = L.lib().scft_iterate_ready(self._h)
+        if r < 0:
+            L.check(r, "scft_iterate_ready")
+        return bool(r)
 
     def iterate_wait(self) -> List[List[IterOut]]:
         n = getattr(self, "_pending", 0)

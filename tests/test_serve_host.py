@@ -55,6 +55,9 @@ class FakeSolver:
         assert not self.pending
         self.pending = n
 
+    def iterate_ready(self):
+        return True
+
     def iterate_wait(self):
         n, self.pending = self.pending, 0
         recs = []
