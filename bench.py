@@ -180,8 +180,9 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
         "algorithmic_bytes_per_step": bytes_iter * B,
         "contour_steps_per_instance_iteration": steps_iter,
         "device_bytes": sv.device_bytes,
-        "kernel": (f"k_chain2d<float,{sv.grid[0]},{sv.grid[2]}> (persistent fused contour loop)" if t["fused_chain"]
-                   else "k_pass_fft + k_pass_dense (per-axis passes)"),
+        "kernel": {1: f"k_chain2d<float,{sv.grid[0]},{sv.grid[2]}> (persistent fused contour loop)",
+                   2: "k_chain3d (64^3 contour loop, one 8-CTA cluster per chain)"}.get(
+                       t["fused_chain"], "k_pass_fft + k_pass_dense (per-axis passes)"),
     }
     res["achieved_gbs"] = bytes_iter * B / (t["prop_ms"] * 1e-3 / steps) / 1e9
     # end to end through the C ABI with pinned host buffers: per step the restart

@@ -262,7 +262,8 @@ typedef struct scft_timing {
     double prop_ms;
     long prop_launches;
     long kernel_launches;
-    int fused_chain;   /* 1: contour steps run in the persistent fused 2D chain kernel */
+    int fused_chain;   /* contour steps run in one persistent launch: 1 the fused 2D chain kernel,
+                          2 the 64^3 cluster kernel; 0 per-axis passes */
     int pad;
 } scft_timing;
 int scft_enable_timing(scft_ctx *ctx, int on);

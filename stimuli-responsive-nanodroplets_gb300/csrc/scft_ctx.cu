@@ -89,8 +89,9 @@ struct scft_ctx {
     InstOps *ops = nullptr;  /* device, room for SCFT_OPS_CAP sets */
     std::vector<int> cap;    /* [B * nchains]: contour slices allocated per chain */
     std::vector<ChainSpec> cs0; /* instance 0's chains: the composition every instance shares */
-    /* fused 2D contour step (scft_step2d.cu) */
+    /* fused contour loops: 2D (scft_step2d.cu), 64^3 clusters (scft_step3d.cu) */
     int fused2d = 0;
+    int fused3d = 0;
     int *order = nullptr; /* chain indices, longest first */
     /* device noise replay (SCFT_NOISE_DRAND48) */
     unsigned long long *rng_in = nullptr;
@@ -418,6 +419,29 @@ static int axis_tables(scft_ctx *c, const Axis &A, double alpha, InstOps &o, int
 
 /* Per-axis pass geometry (shared by every instance) and each operator set's
  * tables. Instances with equal (alphax, alphay, alphaz) share one set. */
+/* The cluster-resident 3D contour loop uses the per-axis spectra of the FFT
+ * passes (spec[x], spec[y], spec[z]); it needs an 8-CTA cluster with ~200 KB
+ * of shared memory per CTA to be schedulable on the device. */
+static int build_fused3d(scft_ctx *c)
+{
+    const scft_derived &d0 = c->der[0];
+    if (c->opt.kernel_path != 0 || c->surf[0].mask || c->fused2d) return SCFT_OK;
+    if (scft_step3d_smem(c->opt.precision, d0.nx, d0.ny, d0.nz) == 0 || c->axes.size() != 3) return SCFT_OK;
+    for (const Axis &A : c->axes)
+        if (A.dirichlet_dense) return SCFT_OK;
+    Step2DArgs a;
+    memset(&a, 0, sizeof(a));
+    const cudaError_t e = scft_launch_step3d(a, 0, c->stream, 1);
+    if (e != cudaSuccess) {
+        /* the cluster cannot be resident on this device (or the query is not
+         * available): the per-axis passes run, which scft_get_timing reports */
+        cudaGetLastError();
+        return SCFT_OK;
+    }
+    c->fused3d = 1;
+    return SCFT_OK;
+}
+
 static int build_axes(scft_ctx *c)
 {
     const scft_derived &d = c->der[0];
@@ -818,7 +842,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         return SCFT_ERR_OOM;
     }
 #undef ALLOC
-    if ((rc = build_axes(c)) || (rc = build_fused2d(c))) {
+    if ((rc = build_axes(c)) || (rc = build_fused2d(c)) || (rc = build_fused3d(c))) {
         scft_ctx_destroy(c);
         return rc;
     }
@@ -893,7 +917,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
         }
     }
 #undef ALLOC
-    if (opt.autotune && !c->fused2d && (rc = autotune_axes(c))) {
+    if (opt.autotune && !c->fused2d && !c->fused3d && (rc = autotune_axes(c))) {
         scft_ctx_destroy(c);
         return rc;
     }
@@ -911,7 +935,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     c->iter.assign(B, 0);
     c->rng.assign(3 * B, 0);
     c->fields_set.assign(B, 0);
-    c->prop_launches_per_iter = c->fused2d ? 1L : (long)(c->maxlen - 1) * (long)c->axes.size();
+    c->prop_launches_per_iter = (c->fused2d || c->fused3d) ? 1L : (long)(c->maxlen - 1) * (long)c->axes.size();
     c->launches_per_iter = c->prop_launches_per_iter + 2 + 6 + (opt.noise_mode == SCFT_NOISE_DRAND48 ? 5 : 0);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
         set_err("context set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1161,7 +1185,7 @@ static PostArgs post_args(scft_ctx *c, const double *noise_dev)
 /* All contour steps of every chain: one launch per axis per step. */
 static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total, int maxlen)
 {
-    if (c->fused2d) {
+    if (c->fused2d || c->fused3d) {
         /* one persistent launch: every chain runs its whole contour loop */
         Step2DArgs a;
         a.chains = chains;
@@ -1170,7 +1194,10 @@ static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total,
         a.s = 0;
         a.s_end = maxlen - 1;
         a.sstride = c->sm;
-        CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0));
+        if (c->fused3d)
+            CK(scft_launch_step3d(a, nchains_total, c->stream, 0));
+        else
+            CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0));
         return SCFT_OK;
     }
     const int npass = (int)c->axes.size();
@@ -1530,7 +1557,7 @@ extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
 {
     if (!c || !t) return SCFT_ERR_PARAM;
     *t = c->last_timing;
-    t->fused_chain = c->fused2d;
+    t->fused_chain = c->fused2d ? 1 : (c->fused3d ? 2 : 0);
     return SCFT_OK;
 }
 

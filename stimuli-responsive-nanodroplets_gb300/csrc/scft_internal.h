@@ -180,6 +180,9 @@ struct Step2DArgs {
 };
 
 size_t scft_step2d_smem(int prec, int nx, int nz);
+/* 64^3 periodic FP32 grids: one 8-CTA cluster per chain (scft_step3d.cu) */
+size_t scft_step3d_smem(int prec, int nx, int ny, int nz);
+cudaError_t scft_launch_step3d(const Step2DArgs &a, int nchains, cudaStream_t st, int configure);
 int scft_step2d_n1(int nx);
 cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
                                int configure);
