@@ -50,6 +50,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(pg, values, device):
+    """Element-wise maximum of per-rank timings (the slowest rank sets the job's
+    time); pg is torch.distributed or None for one process."""
+    if pg is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def job_rate(world: int, per_rank_units: int, ms: float) -> float:
+    """Whole-job throughput: every rank processes per_rank_units per step (weak
+    scaling, replicas), the step time is the maximum over ranks."""
+    return world * per_rank_units / (ms * 1e-3)
+
+
 def workload_surfaces(srn, name: str, batch: int):
     n = int(round(np.sqrt(batch)))
     out = []
@@ -65,6 +82,8 @@ def workload_surfaces(srn, name: str, batch: int):
             out.append(s)
         elif name == "blend3d":
             out.append(srn.configs.blend3d(seed=2 + b))
+        elif name == "bulk3d":
+            out.append(srn.configs.bulk3d_point(chi_ab, chi_ac, srn.configs.PLANES[b % 3], ns=100))
         else:
             raise SystemExit(f"unknown workload {name}")
     return out
@@ -454,15 +473,9 @@ def main():
         return
     f32 = measure_form(srn, surfaces, "fp32", args.steps, args.warmup, local, sync, args.e2e_steps)
     f64 = measure_form(srn, surfaces, "fp64", args.fp64_steps, 1, local, sync, 0)
-    ms = f32["ms_per_step"]
-    if pg is not None:
-        t = torch.tensor([ms, f64["ms_per_step"]], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms, ms64 = float(t[0]), float(t[1])
-    else:
-        ms64 = f64["ms_per_step"]
+    ms, ms64 = max_over_ranks(pg, [f32["ms_per_step"], f64["ms_per_step"]], "cuda")
     B = len(surfaces)
-    value = world * B / (ms * 1e-3)
+    value = job_rate(world, B, ms)
     peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
@@ -483,7 +496,7 @@ def main():
                      "kernel": f32["kernel"],
                      "algorithmic_bytes_per_launch": f32["algorithmic_bytes_per_step"] / f32["prop_launches_per_step"],
                      "launch_ms": f32["prop_ms_per_step"] / f32["prop_launches_per_step"]},
-        "fp64_plain": {"value": world * B / (ms64 * 1e-3), "ms_per_step": ms64, "steps": args.fp64_steps,
+        "fp64_plain": {"value": job_rate(world, B, ms64), "ms_per_step": ms64, "steps": args.fp64_steps,
                        "achieved_gbs": f64["achieved_gbs"], "frac": f64["achieved_gbs"] / peak,
                        "prop_ms_per_step": f64["prop_ms_per_step"], "clocks": f64["clocks"]},
         "detail": {"fp32_prop_ms_per_step": f32["prop_ms_per_step"], "fp32_wall_ms_per_step": f32["wall_ms_per_step"],

@@ -5,25 +5,23 @@
  * (funPDESolver / funPDESolver_periodic, SCFT.c:2310-2412, :2474-2525).
  *
  * The 1 MB slice of a chain lives in the shared memory of an 8-CTA cluster for
- * the chain's whole contour loop: CTA r owns the x planes 8r .. 8r+7 (row pitch
- * 65 floats, plane pitch 64*65+4, so the column and row walks below are free of
- * bank conflicts). Per contour step only q_{s+1} goes to HBM (for the
- * densities) and b is read once; the factor is separable and real and even
- * per axis, so each axis is applied as a real circulant with two real lines
- * packed into one complex line:
- *   z, y (local): one thread per packed line (rows p, p+32 / columns p, p+32 of
- *     one plane), a 64-point FFT in registers (8 x 8 two-factor), E(k)/64, the
- *     inverse FFT, back to shared memory;
- *   x (across the cluster): x = 8c + l with c the owning CTA and l its local
- *     plane; CTA r handles the rows y in [8r, 8r+8) of every plane in two
- *     chunks of four rows: 8-point DFTs over c read straight from the owners'
- *     shared memory (DSMEM), the twiddle W_64^(l k1), a transpose through a
- *     local buffer, 8-point DFTs over l, E(k)/64, the inverse, the transpose
- *     back and the inverse 8-point DFTs over c written back to the owners.
- * Two cluster barriers per step bracket the x phase; everything else is
- * CTA-local. All control flow is uniform over the cluster (one chain per
- * cluster), and a last cluster barrier keeps every CTA's shared memory alive
- * until no other CTA can address it.
+ * the chain's whole contour loop, as 8 planes of 64 rows of 64 z values per CTA
+ * (row pitch 65 floats, plane pitch 64*65+4, so the row and column walks below
+ * are free of bank conflicts). Two distributions alternate:
+ *   D1: CTA r holds x in [8r, 8r+8) as planes, y as rows;
+ *   D2: CTA r holds y in [8r, 8r+8) as planes, x as rows.
+ * The factor is separable, real and even per axis, so each axis is applied as
+ * a real circulant with two real lines packed into one complex line, one
+ * thread per packed line, a 64-point FFT in registers (8 x 8 two-factor),
+ * E(k)/64 and the inverse FFT. z lines and row lines are local in both
+ * distributions, so a step starting in D1 applies z and y, moves to D2 (one
+ * all-to-all through distributed shared memory), applies x, and the next step
+ * does z and x, moves back and applies y. Per step: one exchange (each CTA
+ * pulls 7/8 of its new contents into registers, a cluster barrier, writes them
+ * to its own planes), two cluster barriers, and to HBM only q_{s+1} (for the
+ * densities) with b read once. All control flow is uniform over the cluster
+ * (one chain per cluster), and a last cluster barrier keeps every CTA's shared
+ * memory alive until no other CTA can address it.
  */
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -40,8 +38,7 @@ constexpr int PL = N3 / CL;       /* x planes per CTA */
 constexpr int RP = N3 + 1;        /* row pitch (floats) */
 constexpr int PP = N3 * RP + 4;   /* plane pitch (floats) */
 constexpr int NT = 256;           /* threads per CTA: 8 warps x 32 lanes */
-constexpr int YC = 4;             /* rows per x-phase chunk */
-constexpr int RSTRIDE = 65;       /* complex slots per (row, lane) in the transpose buffer */
+constexpr int UB = 16;            /* float4 loads in flight per thread in the pointwise phases */
 
 struct C2 {
     float x, y;
@@ -50,8 +47,6 @@ struct C2 {
 __device__ __forceinline__ C2 c_add(C2 a, C2 b) { return {a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ C2 c_sub(C2 a, C2 b) { return {a.x - b.x, a.y - b.y}; }
 __device__ __forceinline__ C2 c_mul(C2 a, C2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-/* a * conj(b) */
-__device__ __forceinline__ C2 c_mulc(C2 a, C2 b) { return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y}; }
 template <bool INV>
 __device__ __forceinline__ C2 c_si(C2 a) /* sign*i*a, sign = -1 forward */
 {
@@ -153,33 +148,47 @@ __device__ __forceinline__ void fft64(C2 *v)
     }
 }
 
-/* real circulant along one local axis for two packed lines: x0[i*st], x1[i*st] */
+/* real circulant along one local axis for two packed lines: x0[i*st], x1[i*st].
+ * The inverse transform is the forward one on the conjugate (conj(F(conj Y))),
+ * so one copy of the 64-point FFT serves both directions, and the function is
+ * kept out of line: the three call sites per contour step share one copy of
+ * the code, which keeps the kernel inside the instruction cache. */
 __device__ __forceinline__ void conv_line(float *x0, float *x1, int st, const float *E)
 {
     C2 v[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = C2{x0[i * st], x1[i * st]};
-    fft64<false>(v);
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        fft64<false>(v);
+        if (pass == 0) {
 #pragma unroll
-    for (int k = 0; k < 64; ++k) {
-        const float f = E[k];
-        v[k].x *= f;
-        v[k].y *= f;
+            for (int k = 0; k < 64; ++k) {
+                const float f = E[k];
+                v[k] = C2{v[k].x * f, -(v[k].y * f)}; /* E(k)/64, then conjugate */
+            }
+        }
     }
-    fft64<true>(v);
 #pragma unroll
     for (int i = 0; i < 64; ++i) {
         x0[i * st] = v[i].x;
-        x1[i * st] = v[i].y;
+        x1[i * st] = -v[i].y;
     }
 }
 
 } // namespace
 
 constexpr size_t STEP3D_Q_BYTES = sizeof(float) * PL * PP;
-constexpr size_t STEP3D_R_BYTES = sizeof(C2) * YC * 32 * RSTRIDE;
 constexpr size_t STEP3D_E_BYTES = sizeof(float) * 3 * N3;
-constexpr size_t STEP3D_SMEM = STEP3D_Q_BYTES + STEP3D_R_BYTES + STEP3D_E_BYTES;
+constexpr size_t STEP3D_SMEM = STEP3D_Q_BYTES + STEP3D_E_BYTES;
+
+/* global index of element e (= plane*4096 + row*64 + z) of CTA `rank` in distribution d */
+__device__ __forceinline__ long g_index(int e, int rank, int d)
+{
+    const int p = e >> 12, r = (e >> 6) & 63, z = e & 63;
+    return d == 0 ? (long)(PL * rank + p) * (N3 * N3) + r * N3 + z
+                  : (long)r * (N3 * N3) + (PL * rank + p) * N3 + z;
+}
 
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(Step2DArgs a)
 {
@@ -194,131 +203,102 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(St
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *Q = reinterpret_cast<float *>(smem_raw);
-    C2 *R = reinterpret_cast<C2 *>(smem_raw + STEP3D_Q_BYTES);
-    float *E = reinterpret_cast<float *>(smem_raw + STEP3D_Q_BYTES + STEP3D_R_BYTES); /* x, y, z factors */
+    float *E = reinterpret_cast<float *>(smem_raw + STEP3D_Q_BYTES); /* x, y, z factors */
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long own = (long)rank * PL * N3 * N3; /* first element of this CTA's planes in a slice */
-
     for (int e = tid; e < 3 * N3; e += NT) E[e] = reinterpret_cast<const float *>(cd.ops->spec[e / N3])[e % N3];
 
-    /* Q = b_s . q_s */
+    /* Q = b_s . q_s in D1 */
     {
-        const float4 *q4 = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(cd.q) +
-                                                            (long)a.s * a.sstride + own);
-        const float4 *b4 = reinterpret_cast<const float4 *>(
-            reinterpret_cast<const float *>(a.s < cd.seg_end ? cd.b0 : cd.b1) + own);
-#pragma unroll 4
-        for (int e4 = tid; e4 < PL * N3 * N3 / 4; e4 += NT) {
-            const float4 qv = q4[e4], bv = b4[e4];
-            const int e = 4 * e4, xl = e >> 12, y = (e >> 6) & 63, z = e & 63;
-            float *d = Q + xl * PP + y * RP + z;
-            d[0] = qv.x * bv.x;
-            d[1] = qv.y * bv.y;
-            d[2] = qv.z * bv.z;
-            d[3] = qv.w * bv.w;
+        const float *q = reinterpret_cast<const float *>(cd.q) + (long)a.s * a.sstride;
+        const float *b = reinterpret_cast<const float *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
+        for (int base = tid; base < PL * N3 * N3 / 4; base += NT * UB) {
+            float4 qv[UB], bv[UB];
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+                const long g = g_index(4 * (base + u * NT), rank, 0);
+                qv[u] = __ldg(reinterpret_cast<const float4 *>(q + g));
+                bv[u] = __ldg(reinterpret_cast<const float4 *>(b + g));
+            }
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+                const int e = 4 * (base + u * NT);
+                float *dq = Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63);
+                dq[0] = qv[u].x * bv[u].x;
+                dq[1] = qv[u].y * bv[u].y;
+                dq[2] = qv[u].z * bv[u].z;
+                dq[3] = qv[u].w * bv[u].w;
+            }
         }
     }
     __syncthreads();
 
+    int d = 0; /* current distribution */
     for (int s = a.s; s < s_end; ++s) {
-        /* z: plane `warp`, rows lane and lane+32 */
+        /* z lines: plane `warp`, rows lane and lane+32 */
         {
             float *r0 = Q + warp * PP + lane * RP;
             conv_line(r0, r0 + 32 * RP, 1, E + 2 * N3);
         }
         __syncthreads();
-        /* y: plane `warp`, columns lane and lane+32 */
+        /* row lines (y in D1, x in D2): plane `warp`, columns lane and lane+32 */
         {
             float *c0 = Q + warp * PP + lane;
-            conv_line(c0, c0 + 32, RP, E + N3);
+            conv_line(c0, c0 + 32, RP, E + (d == 0 ? N3 : 0));
         }
-        cl.sync(); /* every CTA's y/z work is done before any x line is read */
-        /* x across the cluster, rows y in [8 rank, 8 rank + 8), packed columns (lane, lane+32) */
-        for (int chunk = 0; chunk < PL / YC; ++chunk) {
-            const int y0 = PL * rank + YC * chunk;
-            {
-                const int l = warp; /* local plane of the inputs this thread combines */
+        cl.sync(); /* every CTA's planes are final for this half of the step */
+        /* exchange: (CTA c, plane p, row 8 rank + j) -> (this CTA, plane j, row 8 c + p); warp w
+         * pulls everything this CTA receives from CTA w, 128 values per thread in registers */
+        {
+            const float *src = cl.map_shared_rank(Q, warp);
+            float v[128];
 #pragma unroll
-                for (int j = 0; j < YC; ++j) {
-                    const int off = l * PP + (y0 + j) * RP + lane;
-                    C2 v[8];
-#pragma unroll
-                    for (int c = 0; c < CL; ++c) {
-                        const float *rq = cl.map_shared_rank(Q, c);
-                        v[c] = C2{rq[off], rq[off + 32]};
-                    }
-                    dft8<false>(v); /* over c -> k1 */
-                    C2 *rr = R + (j * 32 + lane) * RSTRIDE;
-#pragma unroll
-                    for (int k1 = 0; k1 < 8; ++k1) rr[k1 * 8 + l] = (k1 == 0) ? v[0] : c_mul(v[k1], w64<false>(l * k1));
-                }
+            for (int i = 0; i < 128; ++i) {
+                const int p = i >> 4, j = (i >> 1) & 7, zh = i & 1;
+                v[i] = src[p * PP + (PL * rank + j) * RP + 32 * zh + lane];
             }
-            __syncthreads();
-            {
-                const int k1 = warp;
+            cl.sync(); /* every CTA has its inputs: planes may be overwritten */
 #pragma unroll
-                for (int j = 0; j < YC; ++j) {
-                    C2 *rr = R + (j * 32 + lane) * RSTRIDE + k1 * 8;
-                    C2 v[8];
-#pragma unroll
-                    for (int l = 0; l < 8; ++l) v[l] = rr[l];
-                    dft8<false>(v); /* over l -> k2 */
-#pragma unroll
-                    for (int k2 = 0; k2 < 8; ++k2) {
-                        const float f = E[k1 + 8 * k2];
-                        v[k2].x *= f;
-                        v[k2].y *= f;
-                    }
-                    dft8<true>(v); /* k2 -> l */
-#pragma unroll
-                    for (int l = 0; l < 8; ++l) rr[l] = (l == 0) ? v[0] : c_mulc(v[l], w64<false>(l * k1));
-                }
+            for (int i = 0; i < 128; ++i) {
+                const int p = i >> 4, j = (i >> 1) & 7, zh = i & 1;
+                Q[j * PP + (PL * warp + p) * RP + 32 * zh + lane] = v[i];
             }
-            __syncthreads();
-            {
-                const int l = warp;
-#pragma unroll
-                for (int j = 0; j < YC; ++j) {
-                    const C2 *rr = R + (j * 32 + lane) * RSTRIDE;
-                    C2 v[8];
-#pragma unroll
-                    for (int k1 = 0; k1 < 8; ++k1) v[k1] = rr[k1 * 8 + l];
-                    dft8<true>(v); /* k1 -> c */
-                    const int off = l * PP + (y0 + j) * RP + lane;
-#pragma unroll
-                    for (int c = 0; c < CL; ++c) {
-                        float *rq = cl.map_shared_rank(Q, c);
-                        rq[off] = v[c].x;
-                        rq[off + 32] = v[c].y;
-                    }
-                }
-            }
-            __syncthreads(); /* the transpose buffer is reused by the next chunk */
         }
-        cl.sync(); /* every x line is back in its owner's planes */
+        d ^= 1;
+        __syncthreads();
+        /* the remaining axis along the rows of the new distribution */
+        {
+            float *c0 = Q + warp * PP + lane;
+            conv_line(c0, c0 + 32, RP, E + (d == 0 ? N3 : 0));
+        }
+        __syncthreads();
         /* q_{s+1} = b_s . y to HBM; the next step starts from b_{s+1} . q_{s+1} */
         {
-            const float4 *b4 = reinterpret_cast<const float4 *>(
-                reinterpret_cast<const float *>(s < cd.seg_end ? cd.b0 : cd.b1) + own);
-            const bool more = s + 1 < s_end;
+            const float *b = reinterpret_cast<const float *>(s < cd.seg_end ? cd.b0 : cd.b1);
             const float *bn = reinterpret_cast<const float *>(s + 1 < cd.seg_end ? cd.b0 : cd.b1);
-            const bool same = bn == reinterpret_cast<const float *>(s < cd.seg_end ? cd.b0 : cd.b1);
-            const float4 *bn4 = reinterpret_cast<const float4 *>(bn + own);
-            float4 *o4 = reinterpret_cast<float4 *>(reinterpret_cast<float *>(cd.q) + (long)(s + 1) * a.sstride + own);
-#pragma unroll 4
-            for (int e4 = tid; e4 < PL * N3 * N3 / 4; e4 += NT) {
-                const float4 bv = b4[e4];
-                const int e = 4 * e4, xl = e >> 12, y = (e >> 6) & 63, z = e & 63;
-                float *d = Q + xl * PP + y * RP + z;
-                const float4 o = {d[0] * bv.x, d[1] * bv.y, d[2] * bv.z, d[3] * bv.w};
-                o4[e4] = o;
-                if (more) {
-                    const float4 nb = same ? bv : bn4[e4];
-                    d[0] = o.x * nb.x;
-                    d[1] = o.y * nb.y;
-                    d[2] = o.z * nb.z;
-                    d[3] = o.w * nb.w;
+            const bool more = s + 1 < s_end, same = bn == b;
+            float *qn = reinterpret_cast<float *>(cd.q) + (long)(s + 1) * a.sstride;
+            for (int base = tid; base < PL * N3 * N3 / 4; base += NT * UB) {
+                float4 bv[UB], nv[UB];
+#pragma unroll
+                for (int u = 0; u < UB; ++u) {
+                    const long g = g_index(4 * (base + u * NT), rank, d);
+                    bv[u] = __ldg(reinterpret_cast<const float4 *>(b + g));
+                    nv[u] = (more && !same) ? __ldg(reinterpret_cast<const float4 *>(bn + g)) : bv[u];
+                }
+#pragma unroll
+                for (int u = 0; u < UB; ++u) {
+                    const int e = 4 * (base + u * NT);
+                    const long g = g_index(e, rank, d);
+                    float *dq = Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63);
+                    const float4 o = {dq[0] * bv[u].x, dq[1] * bv[u].y, dq[2] * bv[u].z, dq[3] * bv[u].w};
+                    *reinterpret_cast<float4 *>(qn + g) = o;
+                    if (more) {
+                        dq[0] = o.x * nv[u].x;
+                        dq[1] = o.y * nv[u].y;
+                        dq[2] = o.z * nv[u].z;
+                        dq[3] = o.w * nv[u].w;
+                    }
                 }
             }
         }

@@ -1,0 +1,49 @@
+"""The multi-rank path of bench.py on CPU: two gloo ranks reduce their step
+times to the slowest one, the job rate counts every rank's instances, and the
+reference arm runs on rank 0 only."""
+import os
+import sys
+from pathlib import Path
+
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _worker(rank, world, port, out):
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    ms = bench.max_over_ranks(dist, [10.0 + rank, 5.0 - rank], "cpu")
+    out[rank] = ms + [bench.job_rate(world, 256, ms[0])]
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_reduce_to_slowest():
+    world = 2
+    port = 29500 + os.getpid() % 1000
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
+        res = dict(out)
+    for r in range(world):
+        assert res[r][0] == 11.0 and res[r][1] == 5.0
+        assert res[r][2] == pytest.approx(2 * 256 / 0.011)
+
+
+def test_reference_arm_is_rank_zero_only(monkeypatch, capsys):
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class Args:
+        workload, batch, cpu_threads, warmup, steps, ref_max_steps = "film2d", 1, 1, 0, 1, 1
+
+    called = []
+    monkeypatch.setattr(bench, "cpu_sample", lambda *a, **k: called.append(1) or (1.0, 1.0))
+    bench.run_reference(Args, rank=1, world=2)
+    assert not called and capsys.readouterr().out == ""
