@@ -127,6 +127,9 @@ __global__ void k_rng_emit(NoiseArgs n)
     const long G = (long)ip.n_active * n.m;
     long g = n.prefix[(long)b * n.nchunks + chunk];
     if (g >= G) return;
+    /* with MF*DT_NOISE == 0 the draws are not used: only the chunk holding draw
+     * G-1 replays its attempts, to leave the state where the reference's is */
+    if (!write && g + n.counts[(long)b * n.nchunks + chunk] < G) return;
     unsigned long long x = jump_to_chunk(n.state_in[b], (unsigned long long)chunk);
     double x1, w;
     const int na = ip.n_active;

@@ -17,9 +17,11 @@
  *  stage needs no barrier between its loads and stores.
  *  z axis: y = Kz x with Kz symmetric and centrosymmetric (the DST-I factor of
  *  the odd extension for MASK 1, the circulant factor for MASK 0) as two
- *  half-size products on x_k +- x_{NZ-1-k}: each thread keeps its row's
- *  sums and differences in registers and reads operator rows as broadcast
- *  128-bit loads (NZ^2/2 multiply-adds per row).
+ *  half-size products on x_k +- x_{NZ-1-k} (NZ^2/2 multiply-adds per row).
+ *  FP32: a pair of threads shares two rows, each thread holding one half of
+ *  the k range of both rows' sums and differences, so every 128-bit operator
+ *  load feeds both rows; the halves' partial sums meet through a shuffle.
+ *  Otherwise one row per thread with operator rows as broadcast loads.
  */
 #include <cuda_runtime.h>
 
@@ -259,6 +261,76 @@ struct Dft<P, 16, INV> {
     static __device__ __forceinline__ void run(Cx<P> *v) { dft_two_factor<P, 4, 4, INV>(v); }
 };
 
+/* z operator, two lines per thread pair: thread (p, h) holds the k-half h of
+ * the sums and differences of lines 2p and 2p+1, so every operator value it
+ * loads feeds both lines; the two partial sums of an output meet through one
+ * shuffle, and each thread finishes the outputs of its own half. */
+template <int NX, int NZ>
+__device__ __forceinline__ void z_split2(float *X, const float *KA, const float *KB, int tid)
+{
+    constexpr int ZP = NZ + 2, H = NZ / 2, KH = H / 2, KQ = KH / 4;
+    constexpr unsigned MASK = (NX % 32 == 0) ? 0xffffffffu : ((1u << (NX % 32)) - 1u);
+    const int p = tid >> 1, h = tid & 1;
+    float *r0 = X + (2 * p) * ZP;
+    float *r1 = r0 + ZP;
+    const int k0 = h * KH;
+    unsigned long long u0[KH / 2], v0[KH / 2], u1[KH / 2], v1[KH / 2];
+#pragma unroll
+    for (int j = 0; j < KH / 2; ++j) {
+        const int k = k0 + 2 * j;
+        const float2 a0 = *reinterpret_cast<const float2 *>(r0 + k);
+        const float2 a1 = *reinterpret_cast<const float2 *>(r1 + k);
+        const float2 m0 = *reinterpret_cast<const float2 *>(r0 + NZ - 2 - k); /* x[NZ-2-k], x[NZ-1-k] */
+        const float2 m1 = *reinterpret_cast<const float2 *>(r1 + NZ - 2 - k);
+        u0[j] = pack2(a0.x + m0.y, a0.y + m0.x);
+        v0[j] = pack2(a0.x - m0.y, a0.y - m0.x);
+        u1[j] = pack2(a1.x + m1.y, a1.y + m1.x);
+        v1[j] = pack2(a1.x - m1.y, a1.y - m1.x);
+    }
+    for (int jo = 0; jo < KH; ++jo) {
+        unsigned long long s00 = 0ull, s01 = 0ull, s10 = 0ull, s11 = 0ull; /* s[row][line] */
+        unsigned long long d00 = 0ull, d01 = 0ull, d10 = 0ull, d11 = 0ull;
+        const float4 *a0p = reinterpret_cast<const float4 *>(KA + jo * H + k0);
+        const float4 *a1p = reinterpret_cast<const float4 *>(KA + (KH + jo) * H + k0);
+        const float4 *b0p = reinterpret_cast<const float4 *>(KB + jo * H + k0);
+        const float4 *b1p = reinterpret_cast<const float4 *>(KB + (KH + jo) * H + k0);
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) {
+            const float4 a0 = a0p[q], a1 = a1p[q], b0 = b0p[q], b1 = b1p[q];
+            const unsigned long long a0l = pack2(a0.x, a0.y), a0h = pack2(a0.z, a0.w);
+            const unsigned long long a1l = pack2(a1.x, a1.y), a1h = pack2(a1.z, a1.w);
+            const unsigned long long b0l = pack2(b0.x, b0.y), b0h = pack2(b0.z, b0.w);
+            const unsigned long long b1l = pack2(b1.x, b1.y), b1h = pack2(b1.z, b1.w);
+            s00 = fma2(a0h, u0[2 * q + 1], fma2(a0l, u0[2 * q], s00));
+            s01 = fma2(a0h, u1[2 * q + 1], fma2(a0l, u1[2 * q], s01));
+            s10 = fma2(a1h, u0[2 * q + 1], fma2(a1l, u0[2 * q], s10));
+            s11 = fma2(a1h, u1[2 * q + 1], fma2(a1l, u1[2 * q], s11));
+            d00 = fma2(b0h, v0[2 * q + 1], fma2(b0l, v0[2 * q], d00));
+            d01 = fma2(b0h, v1[2 * q + 1], fma2(b0l, v1[2 * q], d01));
+            d10 = fma2(b1h, v0[2 * q + 1], fma2(b1l, v0[2 * q], d10));
+            d11 = fma2(b1h, v1[2 * q + 1], fma2(b1l, v1[2 * q], d11));
+        }
+        /* keep the row of this half (jo for h = 0, KH + jo for h = 1), send the other */
+        const float ks0 = h ? lo2(s10) + hi2(s10) : lo2(s00) + hi2(s00);
+        const float ks1 = h ? lo2(s11) + hi2(s11) : lo2(s01) + hi2(s01);
+        const float kd0 = h ? lo2(d10) + hi2(d10) : lo2(d00) + hi2(d00);
+        const float kd1 = h ? lo2(d11) + hi2(d11) : lo2(d01) + hi2(d01);
+        const float ts0 = h ? lo2(s00) + hi2(s00) : lo2(s10) + hi2(s10);
+        const float ts1 = h ? lo2(s01) + hi2(s01) : lo2(s11) + hi2(s11);
+        const float td0 = h ? lo2(d00) + hi2(d00) : lo2(d10) + hi2(d10);
+        const float td1 = h ? lo2(d01) + hi2(d01) : lo2(d11) + hi2(d11);
+        const float S0 = ks0 + __shfl_xor_sync(MASK, ts0, 1);
+        const float S1 = ks1 + __shfl_xor_sync(MASK, ts1, 1);
+        const float D0 = kd0 + __shfl_xor_sync(MASK, td0, 1);
+        const float D1 = kd1 + __shfl_xor_sync(MASK, td1, 1);
+        const int i = h ? KH + jo : jo;
+        r0[i] = S0 + D0;
+        r0[NZ - 1 - i] = S0 - D0;
+        r1[i] = S1 + D1;
+        r1[NZ - 1 - i] = S1 - D1;
+    }
+}
+
 } // namespace
 
 /* ------------------------------------------------------------------ kernel */
@@ -419,7 +491,10 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     __syncthreads();
 
     /* z: one row per thread, y = A (x + Jx) -> s, B (x - Jx) -> d */
-    {
+    if constexpr (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0) {
+        z_split2<NX, NZ>(reinterpret_cast<float *>(X), reinterpret_cast<const float *>(KA),
+                         reinterpret_cast<const float *>(KB), tid);
+    } else {
         P *row = X + tid * ZP;
         P u[H], v[H];
 #pragma unroll
