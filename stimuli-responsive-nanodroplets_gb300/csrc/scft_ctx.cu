@@ -1153,6 +1153,7 @@ static PostArgs post_args(scft_ctx *c, const double *noise_dev)
     a.species = c->species;
     a.nchains = c->nchains;
     a.nblocks = c->nblocks;
+    a.n_active = c->der[0].n_active;
     a.B = c->B;
     a.nx = c->nx;
     a.ny = c->ny;

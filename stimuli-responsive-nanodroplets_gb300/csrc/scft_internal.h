@@ -137,6 +137,7 @@ struct PostArgs {
     const BlockDesc *blocks;    /* [B][nblocks] */
     const SpeciesDesc *species; /* [B][17] */
     int nchains, nblocks;
+    int n_active;               /* active fields, the same for every instance */
     int B;
     int nx, ny, nz;
     long m, sm;                 /* points, slice stride */

@@ -271,12 +271,15 @@ __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
  * factors sit in shared memory; per-point values stay in registers because all
  * register-array indices are loop counters of fully unrolled loops.
  * Block partials of H, p and (phi_tot-1)^2 go to a.partial. */
-__global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
+template <int NA>
+__global__ void __launch_bounds__(POST_THREADS, (NA <= 5 ? 2 : 1)) k_update(PostArgs a)
 {
     __shared__ double sh[3 * 32];
     __shared__ double coef[SCFT_MAX_BLOCKS];
     __shared__ double chiA[SCFT_NFIELDS][SCFT_NFIELDS];
     __shared__ double pavgA[SCFT_NFIELDS];
+    __shared__ double cA[SCFT_NFIELDS], eA[SCFT_NFIELDS]; /* row sums of chi, of chi . phi_avg */
+    __shared__ double s_ctot;                             /* sum over pairs of chi */
     __shared__ int actf[SCFT_NFIELDS], p0[SCFT_NFIELDS], p1[SCFT_NFIELDS];
     __shared__ int s_na;
     const int b = blockIdx.y;
@@ -304,13 +307,32 @@ __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
         s_na = n;
     }
     __syncthreads();
-    const int na = s_na;
+    /* every instance of a context has NA active fields (checked at creation) */
+    constexpr int na = NA;
     for (int e = threadIdx.x; e < na * na; e += blockDim.x) {
         const int i = e / na, j = e - i * na;
         chiA[i][j] = ip.chi[actf[i]][actf[j]];
     }
     __syncthreads();
-    const double g1 = ip.g1, g2 = ip.g2, dt = ip.dt_noise;
+    if (threadIdx.x < na) {
+        const int i = threadIdx.x;
+        double c = 0.0, e = 0.0;
+        for (int j = 0; j < na; ++j)
+            if (j != i) {
+                c += chiA[i][j];
+                e += chiA[i][j] * pavgA[j];
+            }
+        cA[i] = c;
+        eA[i] = e;
+    }
+    if (threadIdx.x == 0) {
+        double c = 0.0;
+        for (int i = 0; i < na; ++i)
+            for (int j = i + 1; j < na; ++j) c += chiA[i][j];
+        s_ctot = c;
+    }
+    __syncthreads();
+    const double g1 = ip.g1, g2 = ip.g2, g12 = g1 - g2, dt = ip.dt_noise;
     const double inv_na = 1.0 / na;
     const int mask = ip.mask;
     double *w = a.w + (long)b * 14 * a.sm;
@@ -320,13 +342,12 @@ __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
     const bool add_noise = noise && (dt * mf != 0.0);
     double acc[3] = {0.0, 0.0, 0.0};
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < a.m; idx += (long)gridDim.x * blockDim.x) {
-        double ph[SCFT_NFIELDS], wv[SCFT_NFIELDS], dw[SCFT_NFIELDS];
+        double ph[NA], wv[NA], dw[NA];
         double tot = 0.0, sphi = 0.0, wphi = 0.0, hint = 0.0;
         const double pv = w[13 * a.sm + idx];
         bool first_tot = true;
 #pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
+        for (int i = 0; i < NA; ++i) {
             const int f = actf[i], b0 = p0[i], b1 = p1[i];
             /* (raw / 3) * (DS_EFF / Q), then * VOL factor, as funDensity and funVolFrac */
             double v = 0.0;
@@ -343,71 +364,44 @@ __global__ void __launch_bounds__(POST_THREADS) k_update(PostArgs a)
                 first_tot = false;
             }
         }
-        /* free-energy integrand on the pre-update fields */
-        bool first_h = true;
-#pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
-#pragma unroll
-            for (int j = i + 1; j < SCFT_NFIELDS; ++j) {
-                if (j >= na) break;
-                const double t = chiA[i][j] * ph[i] * ph[j];
-                hint = first_h ? t : hint + t;
-                first_h = false;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
-            wphi += wv[i] * ph[i];
-            sphi += ph[i];
-        }
-        hint = hint - wphi - pv * (1.0 - sphi);
-        /* densities out, then reuse ph for phi - phi_avg */
+        /* r = phi - phi_avg over the active fields; t_i = sum_{j != i} chi_ij r_j serves the
+         * field force dw_i = -w_i + p + t_i (SCFT.c:2060-2075), the pair energy
+         * sum_{i<j} chi_ij phi_i phi_j = 1/2 sum_i phi_i (t_i + e_i) with e_i = sum_{j != i}
+         * chi_ij phi_avg_j (SCFT.c:1886-1895), and the correction sum_{f<g} chi_fg sum_{h != f,g}
+         * r_h = R C - sum_f r_f c_f with C = sum_{f<g} chi_fg, c_f = sum_{g != f} chi_fg
+         * (SCFT.c:2076-2091); G = G1 on the diagonal and G1/6 elsewhere, so the mixing sum is
+         * G2 sum_j dw_j + (G1 - G2) dw_i (SCFT.c:2093-2101). Same sums as the reference,
+         * grouped to O(n_active^2) per point. */
+        double r[NA];
         double rsum = 0.0;
 #pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
+        for (int i = 0; i < NA; ++i) {
+            wphi += wv[i] * ph[i];
+            sphi += ph[i];
             phi[(long)actf[i] * a.sm + idx] = ph[i];
-            ph[i] = ph[i] - pavgA[i];
-            rsum += ph[i];
+            r[i] = ph[i] - pavgA[i];
+            rsum += r[i];
         }
         phi[13 * a.sm + idx] = tot;
+        double hpair = 0.0, dsum = 0.0, rc = 0.0;
 #pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
-            double d = -wv[i] + pv;
+        for (int i = 0; i < NA; ++i) {
+            double t = 0.0;
 #pragma unroll
-            for (int j = 0; j < SCFT_NFIELDS; ++j) {
-                if (j >= na) break;
-                if (j != i) d += chiA[i][j] * ph[j];
+            for (int j = 0; j < NA; ++j) {
+                if (j != i) t += chiA[i][j] * r[j];
             }
-            dw[i] = d;
+            hpair += ph[i] * (t + eA[i]);
+            dw[i] = -wv[i] + pv + t;
+            dsum += dw[i];
+            rc += r[i] * cA[i];
         }
-        /* correction: sum over active pairs f<g of chi_fg * sum_{h != f,g} (phi_h - avg_h)
-         * (SCFT.c:2076-2091), written as chi_fg * (R - r_f - r_g) */
-        double corr = 0.0;
-        if (na > 1) {
-#pragma unroll
-            for (int i = 0; i < SCFT_NFIELDS; ++i) {
-                if (i >= na) break;
-#pragma unroll
-                for (int j = i + 1; j < SCFT_NFIELDS; ++j) {
-                    if (j >= na) break;
-                    corr += chiA[i][j] * (rsum - ph[i] - ph[j]);
-                }
-            }
-        }
+        hint = 0.5 * hpair - wphi - pv * (1.0 - sphi);
+        const double corr = na > 1 ? rsum * s_ctot - rc : 0.0;
         double psum = 0.0;
 #pragma unroll
-        for (int i = 0; i < SCFT_NFIELDS; ++i) {
-            if (i >= na) break;
-            double wn = wv[i];
-#pragma unroll
-            for (int j = 0; j < SCFT_NFIELDS; ++j) {
-                if (j >= na) break;
-                wn += (j == i ? g1 : g2) * dw[j];
-            }
+        for (int i = 0; i < NA; ++i) {
+            double wn = wv[i] + (g2 * dsum + g12 * dw[i]);
             if (add_noise) wn += dt * mf * noise[(long)i * a.sm + idx];
             w[(long)actf[i] * a.sm + idx] = wn;
             psum += wn;
@@ -540,7 +534,25 @@ cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_
         k_density<double><<<gd, POST_THREADS, 0, st>>>(a);
     else
         k_density<float><<<gd, POST_THREADS, 0, st>>>(a);
-    k_update<<<dim3(gp, a.B), POST_THREADS, 0, st>>>(a);
+    {
+        const dim3 gu(gp, a.B);
+        switch (a.n_active) {
+        case 1: k_update<1><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 2: k_update<2><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 3: k_update<3><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 4: k_update<4><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 5: k_update<5><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 6: k_update<6><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 7: k_update<7><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 8: k_update<8><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 9: k_update<9><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 10: k_update<10><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 11: k_update<11><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 12: k_update<12><<<gu, POST_THREADS, 0, st>>>(a); break;
+        case 13: k_update<13><<<gu, POST_THREADS, 0, st>>>(a); break;
+        default: return cudaErrorInvalidValue;
+        }
+    }
     k_finalize<<<a.B, POST_THREADS, 0, st>>>(a, gp);
     k_p_shift<<<dim3(gp, a.B), POST_THREADS, 0, st>>>(a);
     return cudaGetLastError();
