@@ -1227,7 +1227,6 @@ static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total,
 static int launch_iteration(scft_ctx *c, const double *noise_dev, int slot)
 {
     PostArgs a = post_args(c, noise_dev);
-    if (c->timing) CK(cudaEventRecord(c->ev[2 + 2 * slot], c->stream));
     CK(scft_post_iter_begin(a, c->opt.precision, c->sms, c->stream));
     if (c->opt.noise_mode == SCFT_NOISE_DRAND48) {
         NoiseArgs na;
@@ -1247,6 +1246,7 @@ static int launch_iteration(scft_ctx *c, const double *noise_dev, int slot)
         na.B = c->B;
         CK(scft_noise_launch(na, c->stream));
     }
+    if (c->timing) CK(cudaEventRecord(c->ev[2 + 2 * slot], c->stream));
     int rc = launch_steps(c, c->chains, c->B * c->nchains, c->maxlen);
     if (rc) return rc;
     if (c->timing) CK(cudaEventRecord(c->ev[3 + 2 * slot], c->stream));

@@ -46,16 +46,34 @@ __device__ __forceinline__ unsigned long long jump_to_chunk(unsigned long long x
     return x;
 }
 
-/* one polar attempt from state x: advances x by two draws, returns accept and (x1, w) */
-__device__ __forceinline__ bool polar_attempt(unsigned long long &x, double &x1, double &w)
+/* x1 = 2 u1 - 1 and w = x1*x1 + x2*x2 from the two draws' states, rounded as
+ * the reference's double expressions are (each product and the sum separately) */
+__device__ __forceinline__ void polar_values(unsigned long long s1, unsigned long long s2, double &x1, double &w)
 {
-    x = lcg_next(x);
-    const double u1 = (double)x * 0x1.0p-48;
-    x = lcg_next(x);
-    const double u2 = (double)x * 0x1.0p-48;
+    const double u1 = (double)s1 * 0x1.0p-48;
+    const double u2 = (double)s2 * 0x1.0p-48;
     x1 = __dsub_rn(__dmul_rn(2.0, u1), 1.0);
     const double x2 = __dsub_rn(__dmul_rn(2.0, u2), 1.0);
     w = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+}
+
+/* One polar attempt from state x: advances x by two draws and returns the
+ * reference's accept decision w < 1. The decision is taken in FP32 (x1, x2
+ * are exact multiples of 2^-47; their FP32 roundings put w within 4e-7 of
+ * its exact value) unless w is within 4e-6 of 1, where the reference's FP64
+ * arithmetic decides. s1, s2: the two draws' states. */
+__device__ __forceinline__ bool polar_attempt(unsigned long long &x, unsigned long long &s1, unsigned long long &s2)
+{
+    s1 = lcg_next(x);
+    s2 = lcg_next(s1);
+    x = s2;
+    const float f1 = (float)((long long)s1 - (1LL << 47)) * 0x1.0p-47f;
+    const float f2 = (float)((long long)s2 - (1LL << 47)) * 0x1.0p-47f;
+    const float wf = f1 * f1 + f2 * f2;
+    if (wf < 1.0f - 4e-6f) return true;
+    if (wf > 1.0f + 4e-6f) return false;
+    double x1, w;
+    polar_values(s1, s2, x1, w);
     return w < 1.0;
 }
 
@@ -66,9 +84,9 @@ __global__ void k_rng_count(NoiseArgs n)
     if (chunk >= n.nchunks || n.state[b].done) return;
     unsigned long long x = jump_to_chunk(n.state_in[b], (unsigned long long)chunk);
     int cnt = 0;
-    double x1, w;
+    unsigned long long s1, s2;
 #pragma unroll 4
-    for (int t = 0; t < RNG_CH; ++t) cnt += polar_attempt(x, x1, w) ? 1 : 0;
+    for (int t = 0; t < RNG_CH; ++t) cnt += polar_attempt(x, s1, s2) ? 1 : 0;
     n.counts[(long)b * n.nchunks + chunk] = cnt;
 }
 
@@ -131,11 +149,13 @@ __global__ void k_rng_emit(NoiseArgs n)
      * G-1 replays its attempts, to leave the state where the reference's is */
     if (!write && g + n.counts[(long)b * n.nchunks + chunk] < G) return;
     unsigned long long x = jump_to_chunk(n.state_in[b], (unsigned long long)chunk);
-    double x1, w;
+    unsigned long long s1, s2;
     const int na = ip.n_active;
     for (int t = 0; t < RNG_CH && g < G; ++t) {
-        if (!polar_attempt(x, x1, w)) continue;
+        if (!polar_attempt(x, s1, s2)) continue;
         if (write) {
+            double x1, w;
+            polar_values(s1, s2, x1, w);
             const double v = x1 * sqrt((-2.0 * log(w)) / w);
             const long p = g / na;
             const int a = (int)(g - p * na);
