@@ -387,7 +387,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "instance-iterations/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded droplet fields)",
+        "data": workload_data(args.workload),
         "config": workload_config(args, surfaces),
         "cpu_baseline": {"value": value, "unit": "instance-iterations/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} steps x 1 iteration of {threads} instances, one per host thread "
@@ -398,11 +398,18 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def workload_data(name: str) -> str:
+    start = {"film2d": "seeded half-disk droplet fields", "bulk3d": "seeded w noise",
+             "bulk2d": "seeded w noise", "blend3d": "seeded w noise"}.get(name, "seeded fields")
+    return f"synthetic ({start}, chi sweep)"
+
+
 def workload_config(args, surfaces):
     s = surfaces[0]
     nx, ny, nz = s.grid()
+    start = "seeded droplet start" if s.MASK else "seeded w-noise start"
     return {"workload": f"{args.workload} {nx}x{ny}x{nz} NS={s.NS} MASK={s.MASK}, {len(surfaces)} instances "
-                        f"(chi_AB x chi_AC sweep), seeded droplet start",
+                        f"(chi_AB x chi_AC sweep), {start}",
             "instances_per_gpu": len(surfaces), "grid": [nx, ny, nz], "ns": s.NS, "mask": s.MASK,
             "l2": "working set larger than L2 (propagators of all instances)",
             "parallelism": "replicas (one batch per GPU)"}
@@ -480,12 +487,14 @@ def main():
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
     if TRAFFIC.exists():
-        traffic = json.loads(TRAFFIC.read_text()).get("fp32", {}).get("traffic_bytes_per_launch")
+        tr = json.loads(TRAFFIC.read_text()).get(args.workload, {})
+        if tr.get("instances") == len(surfaces):
+            traffic = tr.get("traffic_bytes_per_launch")
     line = {
         "metric": METRIC, "value": value, "unit": "instance-iterations/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 propagators, f64 densities/Q/free energy/update",
-        "data": "synthetic (seeded half-disk droplet fields, chi sweep)",
+        "data": workload_data(args.workload),
         "config": workload_config(args, surfaces),
         "e2e": f32.get("e2e"),
         "gpu_launches": f32["gpu_launches"],

@@ -1454,12 +1454,22 @@ extern "C" int scft_get_densities(scft_ctx *c, int b, double *phi13, double *phi
     return SCFT_OK;
 }
 
+/* rows of m doubles between a dense host block and the device's sm-strided
+ * arrays: one plain copy when the two layouts coincide */
+static cudaError_t copy_rows(scft_ctx *c, void *dst, size_t dpitch, const void *src, size_t spitch, size_t rows,
+                             cudaMemcpyKind kind)
+{
+    const size_t width = sizeof(double) * c->m;
+    if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * rows, kind, c->stream);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, c->stream);
+}
+
 extern "C" int scft_set_fields_all(scft_ctx *c, const double *w14_all)
 {
     if (!c || !w14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
-    CK(cudaMemcpy2DAsync(c->w, sizeof(double) * c->sm, w14_all, sizeof(double) * c->m, sizeof(double) * c->m,
-                         (size_t)c->B * 14, cudaMemcpyHostToDevice, c->stream));
+    CK(copy_rows(c, c->w, sizeof(double) * c->sm, w14_all, sizeof(double) * c->m, (size_t)c->B * 14,
+                 cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(c->stream));
     for (int b = 0; b < c->B; ++b) c->fields_set[b] = 1;
     return SCFT_OK;
@@ -1469,8 +1479,8 @@ extern "C" int scft_get_fields_all(scft_ctx *c, double *w14_all)
 {
     if (!c || !w14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
-    CK(cudaMemcpy2DAsync(w14_all, sizeof(double) * c->m, c->w, sizeof(double) * c->sm, sizeof(double) * c->m,
-                         (size_t)c->B * 14, cudaMemcpyDeviceToHost, c->stream));
+    CK(copy_rows(c, w14_all, sizeof(double) * c->m, c->w, sizeof(double) * c->sm, (size_t)c->B * 14,
+                 cudaMemcpyDeviceToHost));
     CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
 }
@@ -1479,8 +1489,8 @@ extern "C" int scft_get_densities_all(scft_ctx *c, double *phi14_all)
 {
     if (!c || !phi14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
-    CK(cudaMemcpy2DAsync(phi14_all, sizeof(double) * c->m, c->phi, sizeof(double) * c->sm, sizeof(double) * c->m,
-                         (size_t)c->B * 14, cudaMemcpyDeviceToHost, c->stream));
+    CK(copy_rows(c, phi14_all, sizeof(double) * c->m, c->phi, sizeof(double) * c->sm, (size_t)c->B * 14,
+                 cudaMemcpyDeviceToHost));
     CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
 }
