@@ -28,9 +28,6 @@
 #include "scft_internal.h"
 
 /* Build switches of the fused chain kernel. */
-#ifndef SCFT_FOLD_B
-#define SCFT_FOLD_B 0 /* 1: multiply the next step's b in the store phase (measured slower) */
-#endif
 #ifndef SCFT_F32X2
 #define SCFT_F32X2 1 /* packed f32x2 FMA in the z phase */
 #endif
@@ -401,7 +398,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     __syncthreads();
 
     /* the first step's input b . q_s; later steps get theirs from the store phase */
-    if (SCFT_FOLD_B) {
+    {
         const P *b_first = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
 #pragma unroll 4
         for (int e = tid; e < NX * NZ2; e += NX) {
@@ -418,26 +415,6 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     const P *bz = reinterpret_cast<const P *>(s < cd.seg_end ? cd.b0 : cd.b1);
     const P *bnext = reinterpret_cast<const P *>(s + 1 < cd.seg_end ? cd.b0 : cd.b1);
     P *qn = reinterpret_cast<P *>(cd.q) + (long)(s + 1) * a.sstride;
-    if (!SCFT_FOLD_B) {
-        /* b . q_s in place, b loads issued a batch at a time */
-        constexpr int PER = NZ2;
-        constexpr int BATCH = (PER % 16 == 0) ? 16 : ((PER % 8 == 0) ? 8 : 4);
-        const T2 *b2p = reinterpret_cast<const T2 *>(bz);
-        for (int j0 = 0; j0 < PER; j0 += BATCH) {
-            T2 bb[BATCH];
-#pragma unroll
-            for (int j = 0; j < BATCH; ++j) bb[j] = b2p[tid + (j0 + j) * NX];
-#pragma unroll
-            for (int j = 0; j < BATCH; ++j) {
-                const int e = tid + (j0 + j) * NX;
-                const int x = e / NZ2, c = e - x * NZ2;
-                T2 &slot = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
-                slot.x *= bb[j].x;
-                slot.y *= bb[j].y;
-            }
-        }
-        __syncthreads();
-    }
     /* A: DFT_N1 over rows N2*n1 + n2 of b . q_s, twiddle, back to rows N2*k1 + n2 */
     for (int w = tid; w < N2 * NZ2; w += NX) {
         const int n2 = w / NZ2, c = w - n2 * NZ2;
@@ -586,14 +563,13 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         }
     }
     __syncthreads();
-    /* q_{s+1} = b . y to HBM for the densities. With SCFT_FOLD_B the next step's
-     * input b_next . q_{s+1} stays in shared memory (b_next differs from b only
-     * at the diblock junction); otherwise q_{s+1} does and the next step
-     * multiplies by its b first. Each thread issues a whole batch of b loads
-     * before using any, so L2 latency is paid once per batch. */
+    /* q_{s+1} = b . y to HBM for the densities; the next step's input
+     * b_next . q_{s+1} stays in shared memory (b_next differs from b only at the
+     * diblock junction), so b is read once per step. Each thread issues all of
+     * its b loads before using any: L2 latency is paid once per step. */
     {
         constexpr int PER = NZ2; /* pairs per thread */
-        constexpr int BATCH = (PER % 16 == 0) ? 16 : ((PER % 8 == 0) ? 8 : 4);
+        constexpr int BATCH = PER;
         const T2 *b2p = reinterpret_cast<const T2 *>(bz);
         const T2 *n2p = reinterpret_cast<const T2 *>(bnext);
         const bool same_b = (bnext == bz);
@@ -610,11 +586,9 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
                 o.x *= bb[j].x;
                 o.y *= bb[j].y;
                 reinterpret_cast<T2 *>(qn)[e] = o;
-                if (SCFT_FOLD_B) {
-                    const T2 nb = same_b ? bb[j] : n2p[e];
-                    o.x *= nb.x;
-                    o.y *= nb.y;
-                }
+                const T2 nb = same_b ? bb[j] : n2p[e];
+                o.x *= nb.x;
+                o.y *= nb.y;
                 slot = o;
             }
         }
