@@ -512,6 +512,9 @@ def main():
                    "contour_steps_per_instance_iteration": f32["contour_steps_per_instance_iteration"],
                    "device_bytes_fp32": f32["device_bytes"]},
     }
+    # the sweep and the serving stream are single-GPU measurements (replicas add nothing to them)
+    if world > 1:
+        args.sweep_n = args.serve_requests = 0
     if args.sweep_n > 0:
         line["sweep"] = measure_sweep(srn, args.sweep_n, args.sweep_tol, args.sweep_max_iter, args.sweep_fp64_iters,
                                       local, sync)
