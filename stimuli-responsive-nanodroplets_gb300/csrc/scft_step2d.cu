@@ -95,6 +95,25 @@ template <typename P>
 __device__ __forceinline__ Cx<P> cadd(Cx<P> a, Cx<P> b) { return {a.x + b.x, a.y + b.y}; }
 template <typename P>
 __device__ __forceinline__ Cx<P> csub(Cx<P> a, Cx<P> b) { return {a.x - b.x, a.y - b.y}; }
+/* FP32: one packed f32x2 instruction per complex add or subtract */
+template <>
+__device__ __forceinline__ Cx<float> cadd(Cx<float> a, Cx<float> b)
+{
+    Cx<float> r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+template <>
+__device__ __forceinline__ Cx<float> csub(Cx<float> a, Cx<float> b)
+{
+    Cx<float> r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
 template <typename P, bool INV>
 __device__ __forceinline__ Cx<P> mul_si(Cx<P> a) /* sign*i*a, sign = -1 forward */
 {

@@ -44,8 +44,23 @@ struct C2 {
     float x, y;
 };
 
-__device__ __forceinline__ C2 c_add(C2 a, C2 b) { return {a.x + b.x, a.y + b.y}; }
-__device__ __forceinline__ C2 c_sub(C2 a, C2 b) { return {a.x - b.x, a.y - b.y}; }
+/* complex add and subtract as one packed f32x2 instruction each */
+__device__ __forceinline__ C2 c_add(C2 a, C2 b)
+{
+    C2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ C2 c_sub(C2 a, C2 b)
+{
+    C2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
 __device__ __forceinline__ C2 c_mul(C2 a, C2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 template <bool INV>
 __device__ __forceinline__ C2 c_si(C2 a) /* sign*i*a, sign = -1 forward */
