@@ -166,7 +166,8 @@ def algorithmic_bytes(solver, psize: int) -> float:
     return float(steps) * 3 * psize * solver.M, steps
 
 
-def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device: int, sync, e2e_steps: int):
+def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device: int, sync, e2e_steps: int,
+                 e2e_parts: int = 8):
     B = len(surfaces)
     sv = srn.Solver(surfaces, precision=precision, device=device, noise="device")
     init = [initial_fields(srn, s, 1000 + b) for b, s in enumerate(surfaces)]
@@ -206,34 +207,68 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
     res["achieved_gbs"] = bytes_iter * B / (t["prop_ms"] * 1e-3 / steps) / 1e9
     # end to end through the C ABI with pinned host buffers: per step the restart
     # fields of every instance go in, one iteration runs, fields and densities
-    # come back (one strided copy each way for the whole batch)
+    # come back. The batch is split into `e2e_parts` contexts on their own streams
+    # and software-pipelined: a part's transfers of step k overlap the other
+    # parts' iterations (each part still waits for its own outputs of step k-1
+    # before sending step k's inputs).
     if e2e_steps > 0:
         import ctypes as C
         import torch
         M = sv.M
-        w_host = torch.empty((B, 14, M), dtype=torch.float64, pin_memory=True).numpy()
-        phi_host = torch.empty((B, 14, M), dtype=torch.float64, pin_memory=True).numpy()
-        for b in range(B):
-            w_host[b] = sv.get_fields(b)
-        sv.enable_timing(False)
+        fields0 = [sv.get_fields(b) for b in range(B)]
+        sv.close()
         Lm = importlib.import_module(f"{PKG}._lib")
         dp = C.POINTER(C.c_double)
         lib = Lm.lib()
-        recs = (Lm.CIterOut * B)()
-        wp = w_host.ctypes.data_as(dp)
-        pp = phi_host.ctypes.data_as(dp)
+        bounds = np.linspace(0, B, e2e_parts + 1).astype(int)
+        parts = []
+        for k in range(e2e_parts):
+            lo, hi = int(bounds[k]), int(bounds[k + 1])
+            psv = srn.Solver(surfaces[lo:hi], precision=precision, device=device, noise="device")
+            for j, b in enumerate(range(lo, hi)):
+                if init[b][1] is not None:
+                    psv.set_masks(init[b][1], j)
+                psv.set_iteration(start_iteration(surfaces[b]) + warmup, j)
+                psv.set_rng((11 + b, 22, 33), j)
+            w_host = torch.empty((hi - lo, 14, M), dtype=torch.float64, pin_memory=True).numpy()
+            phi_host = torch.empty((hi - lo, 14, M), dtype=torch.float64, pin_memory=True).numpy()
+            for j, b in enumerate(range(lo, hi)):
+                w_host[j] = fields0[b]
+            parts.append((psv, w_host, phi_host, (Lm.CIterOut * (hi - lo))()))
+
+        def enqueue(part):
+            psv, w_host, phi_host, _ = part
+            Lm.check(lib.scft_set_fields_all_async(psv._h, w_host.ctypes.data_as(dp)), "set_fields_all_async")
+            Lm.check(lib.scft_iterate_async(psv._h, 1), "iterate_async")
+            Lm.check(lib.scft_get_fields_all_async(psv._h, w_host.ctypes.data_as(dp)), "get_fields_all_async")
+            Lm.check(lib.scft_get_densities_all_async(psv._h, phi_host.ctypes.data_as(dp)), "get_densities_all_async")
+
+        def wait(part):
+            Lm.check(lib.scft_iterate_wait(part[0]._h, part[3]), "iterate_wait")
+
+        for part in parts:  # one untimed round: graph capture, first touch
+            enqueue(part)
+        for part in parts:
+            wait(part)
         sync()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            Lm.check(lib.scft_set_fields_all(sv._h, wp), "set_fields_all")
-            Lm.check(lib.scft_iterate(sv._h, 1, None, recs), "iterate")
-            Lm.check(lib.scft_get_fields_all(sv._h, wp), "get_fields_all")
-            Lm.check(lib.scft_get_densities_all(sv._h, pp), "get_densities_all")
+        for part in parts:
+            enqueue(part)
+        for _ in range(e2e_steps - 1):
+            for part in parts:
+                wait(part)
+                enqueue(part)
+        for part in parts:
+            wait(part)
         sync()
         e2e = time.perf_counter() - t0
+        for part in parts:
+            part[0].close()
         res["e2e"] = {"value": B * e2e_steps / e2e, "unit": "instance-iterations/s",
                       "h2d_bytes_per_step": B * 14 * M * 8,
-                      "d2h_bytes_per_step": B * (14 + 14) * M * 8 + B * C.sizeof(Lm.CIterOut)}
+                      "d2h_bytes_per_step": B * (14 + 14) * M * 8 + B * C.sizeof(Lm.CIterOut),
+                      "contexts": e2e_parts, "steps": e2e_steps}
+        return res
     sv.close()
     return res
 
@@ -424,7 +459,8 @@ def main():
     ap.add_argument("--workload", default="film2d")
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--fp64-steps", type=int, default=5)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-parts", type=int, default=8, help="contexts the e2e batch is pipelined over")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--cpu-iters", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=10)
@@ -478,7 +514,7 @@ def main():
         print(f"profile case: {len(surfaces)} instances, F[0] = {out[0][0].free_energy:.12f}")
         sv.close()
         return
-    f32 = measure_form(srn, surfaces, "fp32", args.steps, args.warmup, local, sync, args.e2e_steps)
+    f32 = measure_form(srn, surfaces, "fp32", args.steps, args.warmup, local, sync, args.e2e_steps, args.e2e_parts)
     f64 = measure_form(srn, surfaces, "fp64", args.fp64_steps, 1, local, sync, 0)
     ms, ms64 = max_over_ranks(pg, [f32["ms_per_step"], f64["ms_per_step"]], "cuda")
     B = len(surfaces)

@@ -235,6 +235,14 @@ int scft_get_densities(scft_ctx *ctx, int instance, double *phi13, double *phi_t
 int scft_set_fields_all(scft_ctx *ctx, const double *w14_all);
 int scft_get_fields_all(scft_ctx *ctx, double *w14_all);
 int scft_get_densities_all(scft_ctx *ctx, double *phi14_all);
+/* The same transfers enqueued on the context's stream without waiting, in
+ * order with scft_iterate_async; the host buffers must stay valid (and, to
+ * overlap with other contexts' work, be pinned) until scft_sync or
+ * scft_iterate_wait returns. */
+int scft_set_fields_all_async(scft_ctx *ctx, const double *w14_all);
+int scft_get_fields_all_async(scft_ctx *ctx, double *w14_all);
+int scft_get_densities_all_async(scft_ctx *ctx, double *phi14_all);
+int scft_sync(scft_ctx *ctx);
 
 /* Unit entry point: contour steps of one block, as funPDESolver does
  * (SCFT.c:2310-2412) in this context's geometry and precision. q0 is the

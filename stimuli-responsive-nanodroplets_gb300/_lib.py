@@ -154,6 +154,10 @@ def lib() -> C.CDLL:
         "scft_set_fields_all": (I, [VP, dp]),
         "scft_get_fields_all": (I, [VP, dp]),
         "scft_get_densities_all": (I, [VP, dp]),
+        "scft_set_fields_all_async": (I, [VP, dp]),
+        "scft_get_fields_all_async": (I, [VP, dp]),
+        "scft_get_densities_all_async": (I, [VP, dp]),
+        "scft_sync": (I, [VP]),
         "scft_propagate": (I, [VP, dp, dp, I, dp]),
         "scft_propagate_static": (I, [VP, dp, dp, I, dp]),
         "scft_static_scratch_bytes": (C.c_size_t, []),

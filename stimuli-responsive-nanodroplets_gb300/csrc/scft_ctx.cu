@@ -1464,35 +1464,58 @@ static cudaError_t copy_rows(scft_ctx *c, void *dst, size_t dpitch, const void *
     return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, c->stream);
 }
 
-extern "C" int scft_set_fields_all(scft_ctx *c, const double *w14_all)
+extern "C" int scft_set_fields_all_async(scft_ctx *c, const double *w14_all)
 {
     if (!c || !w14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
     CK(copy_rows(c, c->w, sizeof(double) * c->sm, w14_all, sizeof(double) * c->m, (size_t)c->B * 14,
                  cudaMemcpyHostToDevice));
-    CK(cudaStreamSynchronize(c->stream));
     for (int b = 0; b < c->B; ++b) c->fields_set[b] = 1;
     return SCFT_OK;
 }
 
-extern "C" int scft_get_fields_all(scft_ctx *c, double *w14_all)
+extern "C" int scft_get_fields_all_async(scft_ctx *c, double *w14_all)
 {
     if (!c || !w14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
     CK(copy_rows(c, w14_all, sizeof(double) * c->m, c->w, sizeof(double) * c->sm, (size_t)c->B * 14,
                  cudaMemcpyDeviceToHost));
-    CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
 }
 
-extern "C" int scft_get_densities_all(scft_ctx *c, double *phi14_all)
+extern "C" int scft_get_densities_all_async(scft_ctx *c, double *phi14_all)
 {
     if (!c || !phi14_all) return SCFT_ERR_PARAM;
     cudaSetDevice(c->device);
     CK(copy_rows(c, phi14_all, sizeof(double) * c->m, c->phi, sizeof(double) * c->sm, (size_t)c->B * 14,
                  cudaMemcpyDeviceToHost));
+    return SCFT_OK;
+}
+
+extern "C" int scft_sync(scft_ctx *c)
+{
+    if (!c) return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
     CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
+}
+
+extern "C" int scft_set_fields_all(scft_ctx *c, const double *w14_all)
+{
+    int rc = scft_set_fields_all_async(c, w14_all);
+    return rc ? rc : scft_sync(c);
+}
+
+extern "C" int scft_get_fields_all(scft_ctx *c, double *w14_all)
+{
+    int rc = scft_get_fields_all_async(c, w14_all);
+    return rc ? rc : scft_sync(c);
+}
+
+extern "C" int scft_get_densities_all(scft_ctx *c, double *phi14_all)
+{
+    int rc = scft_get_densities_all_async(c, phi14_all);
+    return rc ? rc : scft_sync(c);
 }
 
 extern "C" int scft_propagate(scft_ctx *c, const double *q0, const double *w, int steps, double *q_out)

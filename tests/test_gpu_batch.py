@@ -211,3 +211,39 @@ def test_batch_run_to_tolerance(srn):
             _, tot = b.get_densities(i)
             assert res[i].converged and res[i].rms < tols[i] and res[i].iterations <= 150
             assert abs(np.sqrt(np.mean((tot - 1.0) ** 2)) - res[i].rms) <= 1e-12
+
+
+def test_async_batched_transfers_match_sync(srn):
+    """scft_*_all_async + scft_iterate_async / _wait give what the blocking calls give."""
+    import ctypes as C
+    import importlib
+    L = importlib.import_module("stimuli-responsive-nanodroplets_gb300._lib")
+    surfaces = [_film(srn, 32, 16, 50, 14.0 + 4 * b) for b in range(3)]
+    w0 = np.stack([srn.configs.droplet_fields(s, seed=30 + b, radius=1.0) for b, s in enumerate(surfaces)])
+    m = srn.configs.substrate_mask(surfaces[0])
+    dp = C.POINTER(C.c_double)
+    out = []
+    for mode in ("sync", "async"):
+        with srn.Solver(surfaces, precision="fp32", noise="device") as sv:
+            for b in range(3):
+                sv.set_masks(m, b)
+                sv.set_iteration(1, b)
+                sv.set_rng((b, 1, 2), b)
+            w = np.ascontiguousarray(w0.copy())
+            phi = np.zeros_like(w)
+            lib = L.lib()
+            for _ in range(4):
+                if mode == "sync":
+                    L.check(lib.scft_set_fields_all(sv._h, w.ctypes.data_as(dp)), "set")
+                    sv.iterate(1)
+                    L.check(lib.scft_get_fields_all(sv._h, w.ctypes.data_as(dp)), "get")
+                    L.check(lib.scft_get_densities_all(sv._h, phi.ctypes.data_as(dp)), "getphi")
+                else:
+                    L.check(lib.scft_set_fields_all_async(sv._h, w.ctypes.data_as(dp)), "set")
+                    sv.iterate_async(1)
+                    L.check(lib.scft_get_fields_all_async(sv._h, w.ctypes.data_as(dp)), "get")
+                    L.check(lib.scft_get_densities_all_async(sv._h, phi.ctypes.data_as(dp)), "getphi")
+                    sv.iterate_wait()
+            out.append((w.copy(), phi.copy()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

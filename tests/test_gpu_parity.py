@@ -184,3 +184,35 @@ def test_fp32_form_error_bounds(case, srn, golden):
     for row in g["free_energy"]:
         rec = by_iter[int(row[0])]
         assert abs(rec.free_energy - row[1]) <= 3e-6 * max(1.0, abs(row[1])), (case, rec.free_energy, row[1])
+
+
+def test_film3d_mask_vs_oracle(srn, oracle_mod):
+    """A 3D thin film (MASK 1: Dirichlet z, brush on the k = 0 plane), 16x10x12,
+    two iterations of the plain form against the oracle."""
+    S = srn.configs.film2d(nx=16, nz=12, ns=30, iters=2)
+    S.LY = 10 * 0.125  # (LY = 1.0 would collapse the axis to one point, SCFT.c:103-105)
+    nx, ny, nz = S.grid()
+    assert (nx, ny, nz) == (16, 10, 12)
+    i, j, k = srn.configs.idx_coords(nx, ny, nz)
+    rng = np.random.default_rng(11)
+    w = np.zeros((14, nx * ny * nz))
+    for f in (0, 1, 2, 10):
+        w[f] = rng.uniform(-0.5, 0.5, nx * ny * nz) + (2.0 if f < 2 else 0.0) * np.cos(2 * np.pi * i / nx)
+    m = srn.configs.substrate_mask(S)
+    o = oracle_mod.Oracle(S)
+    o.set_fields(w)
+    o.set_masks(m)
+    o.set_iter(1)
+    rec = o.iterate(2)
+    with srn.Solver(S, precision="fp64") as sv:
+        sv.set_fields(w)
+        sv.set_masks(m)
+        sv.set_iteration(1)
+        out = sv.iterate(2)
+        phi, _ = sv.get_densities()
+    for k2 in range(2):
+        assert abs(out[k2][0].free_energy - rec[k2, 1]) <= F_RTOL * abs(rec[k2, 1])
+    ophi, _ = o.densities()
+    scale = np.maximum(np.abs(ophi).max(axis=1, keepdims=True), 1e-300)
+    assert np.all(np.abs(phi - ophi) <= PHI_RTOL * scale + 1e-15)
+    o.close()
