@@ -59,6 +59,7 @@ template <>
 struct V4<double> {
     using T = double2;
     static constexpr int W = 2;
+    static_assert(W * sizeof(double) == sizeof(T), "one 16-byte load");
 };
 
 template <typename P>
@@ -179,14 +180,14 @@ __device__ __forceinline__ unsigned long long pack2(float lo, float hi)
 }
 __device__ __forceinline__ float lo2(unsigned long long r)
 {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+    float lo;
+    asm("mov.b64 {%0, _}, %1;" : "=f"(lo) : "l"(r));
     return lo;
 }
 __device__ __forceinline__ float hi2(unsigned long long r)
 {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+    float hi;
+    asm("mov.b64 {_, %0}, %1;" : "=f"(hi) : "l"(r));
     return hi;
 }
 /* c + a * b lane-wise, round to nearest */
