@@ -250,6 +250,15 @@ int scft_sync(scft_ctx *ctx);
  * steps+1 slices (contour-major, slice 0 = q0). */
 int scft_propagate(scft_ctx *ctx, const double *q0, const double *w, int steps, double *q_out);
 
+/* Unit entry point: funMultiplyQs + funDensity (SCFT.c:2243-2308) on host
+ * propagators qf, qb (len slices of M doubles, contour-major as scft_propagate
+ * returns them): phi = (sum_s w_s qf[s] qb[len-1-s] / 3) * (DS_EFF / q), the
+ * reference's Simpson weights over s in [start, stop], DS_EFF = 1/(len-1). The
+ * propagators are held in the context's precision and summed as the iteration
+ * does (FP64, or double-float for FP32 propagators). */
+int scft_density(scft_ctx *ctx, const double *qf, const double *qb, int len, int start, int stop, double q,
+                 double *phi);
+
 /* scft_propagate for callers that must not allocate device memory at run time
  * (hosts whose memory pools already own the device, code that cannot accept the
  * device synchronisation cudaMalloc/cudaFree may cause or an allocation failure

@@ -47,6 +47,7 @@ def lib():
         L.orc_get_densities.argtypes = [vp, dp, dp]
         L.orc_derived.argtypes = [vp, C.POINTER(C.c_int), dp]
         L.orc_propagate.argtypes = [vp, dp, dp, C.c_int, dp]
+        L.orc_density.argtypes = [vp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, dp]
         L.orc_iterate.restype = C.c_int
         L.orc_iterate.argtypes = [vp, C.c_int, dp]
         L.orc_surface_size.restype = C.c_size_t
@@ -140,4 +141,12 @@ class Oracle:
         w = np.ascontiguousarray(w, dtype=np.float64)
         out = np.empty((steps + 1, self.M))
         lib().orc_propagate(self._h, _dp(q0), _dp(w), int(steps), _dp(out))
+        return out
+
+    def density(self, qf, qb, start, stop, q):
+        """funMultiplyQs + funDensity for one block (qf, qb: [len][M])."""
+        qf = np.ascontiguousarray(qf, dtype=np.float64)
+        qb = np.ascontiguousarray(qb, dtype=np.float64)
+        out = np.empty(self.M)
+        lib().orc_density(self._h, _dp(qf), _dp(qb), int(qf.shape[0]), int(start), int(stop), float(q), _dp(out))
         return out

@@ -431,6 +431,26 @@ static void density(orc *o, int start, int stop, double *phir, const double *qc,
     }
 }
 
+/* funMultiplyQs then funDensity for one block of a chain of len slices given
+ * contour-major ([len][M]) as the unit entry points take them (SCFT.c:2243-2308) */
+void orc_density(orc *o, const double *qf, const double *qb, int len, int start, int stop, double Q, double *phi)
+{
+    const long M = o->M;
+    double *a = malloc(sizeof(double) * M * len), *b = malloc(sizeof(double) * M * len);
+    double *qc = malloc(sizeof(double) * M * len);
+    for (int s = 0; s < len; ++s)
+        for (long idx = 0; idx < M; ++idx) {
+            a[s + (long)len * idx] = qf[(long)s * M + idx];
+            b[s + (long)len * idx] = qb[(long)s * M + idx];
+        }
+    o->NS_EFF = len;
+    multiply(o, a, b, qc);
+    density(o, start, stop, phi, qc, Q);
+    free(a);
+    free(b);
+    free(qc);
+}
+
 static double polar_gauss(unsigned short st[3]) /* funGaussDev, SCFT.c:1769-1782 */
 {
     double x1, x2, w;

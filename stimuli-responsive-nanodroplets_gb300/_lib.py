@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
         "scft_get_densities_all_async": (I, [VP, dp]),
         "scft_sync": (I, [VP]),
         "scft_propagate": (I, [VP, dp, dp, I, dp]),
+        "scft_density": (I, [VP, dp, dp, I, I, I, D, dp]),
         "scft_propagate_static": (I, [VP, dp, dp, I, dp]),
         "scft_static_scratch_bytes": (C.c_size_t, []),
         "scft_enable_timing": (I, [VP, I]),

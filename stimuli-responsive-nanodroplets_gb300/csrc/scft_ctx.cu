@@ -1580,6 +1580,86 @@ extern "C" int scft_propagate(scft_ctx *c, const double *q0, const double *w, in
     return rc;
 }
 
+extern "C" int scft_density(scft_ctx *c, const double *qf, const double *qb, int len, int start, int stop, double q,
+                            double *phi)
+{
+    if (!c || !qf || !qb || !phi || len < 2 || start < 0 || stop <= start || stop > len - 1 || !(q != 0.0))
+        return SCFT_ERR_PARAM;
+    cudaSetDevice(c->device);
+    const size_t sm = c->sm, m = c->m, ps = (size_t)c->psize;
+    double *stage = nullptr, *raw = nullptr;
+    void *qfd = nullptr, *qbd = nullptr;
+    ChainDesc *cdd = nullptr;
+    BlockDesc *bdd = nullptr;
+    InstState *std_ = nullptr;
+    int rc = SCFT_OK;
+    cudaError_t e = cudaMalloc(&stage, sizeof(double) * sm * len);
+    if (e == cudaSuccess) e = cudaMalloc(&raw, sizeof(double) * sm);
+    if (e == cudaSuccess) e = cudaMalloc(&qfd, ps * sm * len);
+    if (e == cudaSuccess) e = cudaMalloc(&qbd, ps * sm * len);
+    if (e == cudaSuccess) e = cudaMalloc(&cdd, 2 * sizeof(ChainDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&bdd, sizeof(BlockDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&std_, sizeof(InstState));
+    if (e != cudaSuccess) {
+        set_err("scft_density: allocation failed: %s", cudaGetErrorString(e));
+        rc = SCFT_ERR_OOM;
+    }
+    if (rc == SCFT_OK) {
+        ChainDesc cd[2];
+        memset(cd, 0, sizeof(cd));
+        cd[0].q = qfd;
+        cd[1].q = qbd;
+        cd[0].len = cd[1].len = len;
+        BlockDesc bd = {0, 1, start, stop, len, 0, 0, 0};
+        InstState st;
+        memset(&st, 0, sizeof(st));
+        e = cudaMemcpyAsync(cdd, cd, sizeof(cd), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(bdd, &bd, sizeof(bd), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(std_, &st, sizeof(st), cudaMemcpyHostToDevice, c->stream);
+        const double *src[2] = {qf, qb};
+        void *dst[2] = {qfd, qbd};
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            e = cudaMemcpy2DAsync(stage, sizeof(double) * sm, src[k], sizeof(double) * m, sizeof(double) * m, len,
+                                  cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess) e = scft_convert(c->opt.precision, stage, dst[k], (long)(sm * len), 1, c->stream);
+        }
+        if (e == cudaSuccess) {
+            PostArgs a;
+            memset(&a, 0, sizeof(a));
+            a.state = std_;
+            a.chains = cdd;
+            a.blocks = bdd;
+            a.nchains = 2;
+            a.nblocks = 1;
+            a.B = 1;
+            a.m = c->m;
+            a.sm = c->sm;
+            a.raw = raw;
+            e = scft_density_launch(a, c->opt.precision, c->sms, c->stream);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(phi, raw, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            set_err("scft_density: %s", cudaGetErrorString(e));
+            rc = SCFT_ERR_CUDA;
+        }
+    }
+    if (rc == SCFT_OK) {
+        /* (sum / 3) * (DS_EFF / Q), SCFT.c:2298-2299 */
+        const double f = (1.0 / (len - 1)) / q;
+        for (size_t i = 0; i < m; ++i) phi[i] = (phi[i] / 3.0) * f;
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(stage);
+    cudaFree(raw);
+    cudaFree(qfd);
+    cudaFree(qbd);
+    cudaFree(cdd);
+    cudaFree(bdd);
+    cudaFree(std_);
+    return rc;
+}
+
 extern "C" int scft_enable_timing(scft_ctx *c, int on)
 {
     if (!c) return SCFT_ERR_PARAM;

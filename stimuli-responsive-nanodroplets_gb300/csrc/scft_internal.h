@@ -163,6 +163,8 @@ struct PostArgs {
 cudaError_t scft_post_iter_begin(const PostArgs &a, int prec, int sms, cudaStream_t st);
 cudaError_t scft_post_mark_start(const PostArgs &a, cudaStream_t st);
 cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_t st);
+/* k_density alone (the unit entry point scft_density) */
+cudaError_t scft_density_launch(const PostArgs &a, int prec, int sms, cudaStream_t st);
 int scft_post_nparts(long m, int sms);
 cudaError_t scft_convert(int prec, const double *src, void *dst, long n, int to_p, cudaStream_t st);
 cudaError_t scft_boltz_one(int prec, const double *w, void *bz, double ds, long m, cudaStream_t st);

@@ -578,6 +578,17 @@ cudaError_t scft_post_mark_start(const PostArgs &a, cudaStream_t st)
 
 int scft_post_nparts(long m, int sms) { return grid_for(m, sms); }
 
+cudaError_t scft_density_launch(const PostArgs &a, int prec, int sms, cudaStream_t st)
+{
+    const int vw = prec == SCFT_PREC_FP64 ? 2 : 4;
+    dim3 gd(grid_for((a.m + vw - 1) / vw, sms), a.nblocks, a.B);
+    if (prec == SCFT_PREC_FP64)
+        k_density<double><<<gd, POST_THREADS, 0, st>>>(a);
+    else
+        k_density<float><<<gd, POST_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_t st)
 {
     const int gp = grid_for(a.m, sms);

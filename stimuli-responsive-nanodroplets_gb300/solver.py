@@ -234,6 +234,16 @@ class Solver:
         L.check(L.lib().scft_propagate(self._h, _dp(q0), _dp(w), int(steps), _dp(out)), "scft_propagate")
         return out
 
+    def density(self, qf: np.ndarray, qb: np.ndarray, start: int, stop: int, q: float) -> np.ndarray:
+        """funMultiplyQs + funDensity for one block (unit entry point)."""
+        qf = np.ascontiguousarray(qf, dtype=np.float64)
+        qb = np.ascontiguousarray(qb, dtype=np.float64)
+        n = qf.shape[0]
+        out = np.empty(self.M)
+        L.check(L.lib().scft_density(self._h, _dp(qf), _dp(qb), int(n), int(start), int(stop), float(q), _dp(out)),
+                "scft_density")
+        return out
+
     def enable_timing(self, on: bool = True):
         L.check(L.lib().scft_enable_timing(self._h, int(on)), "scft_enable_timing")
 

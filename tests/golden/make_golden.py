@@ -221,6 +221,39 @@ def kat_prop(tag: str, s, steps: int, seed: int):
     print(f"kat_prop_{tag}: {steps} steps on {nx}x{ny}x{nz}")
 
 
+def kat_density(tag: str, s, ns: int, blocks, seed: int):
+    """funMultiplyQs + funDensity on seeded propagators through a shared build of
+    the reference; blocks: (start, stop) pairs of one chain of ns slices."""
+    d = WORK / f"kat_{tag}"
+    if d.exists():
+        shutil.rmtree(d)
+    so = obuild.build_reference(d, s.to_parameters_h(), full_precision=False, shared=True)
+    L = C.CDLL(str(so))
+    nx, ny, nz = s.grid()
+    M = nx * ny * nz
+    for name, val in (("NX", nx), ("NY", ny), ("NZ", nz), ("NS_EFF", ns)):
+        C.c_int.in_dll(L, name).value = val
+    rng = np.random.default_rng(seed)
+    qf = 1.0 + 0.3 * rng.random((ns, M))
+    qb = 1.0 + 0.3 * rng.random((ns, M))
+    qr = np.ascontiguousarray(qf.T).reshape(-1)      # AoS: q[s + NS * idx]
+    qm = np.ascontiguousarray(qb.T).reshape(-1)
+    qc = np.zeros(M * ns)
+    dp = C.POINTER(C.c_double)
+    L.funMultiplyQs.argtypes = [dp, dp, dp]
+    L.funMultiplyQs(qr.ctypes.data_as(dp), qm.ctypes.data_as(dp), qc.ctypes.data_as(dp))
+    L.funDensity.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double]
+    Q = 1.0 + 0.1 * float(rng.random())
+    phis = []
+    for start, stop in blocks:
+        phi = np.zeros(M)
+        L.funDensity(int(start), int(stop), phi.ctypes.data_as(dp), qc.ctypes.data_as(dp), C.c_double(Q))
+        phis.append(phi)
+    np.savez_compressed(GOLD / f"kat_density_{tag}.npz", grid=np.array([nx, ny, nz]), qf=qf, qb=qb, Q=Q,
+                        blocks=np.array(blocks), phi=np.array(phis))
+    print(f"kat_density_{tag}: {ns} slices on {nx}x{ny}x{nz}, blocks {blocks}")
+
+
 def main():
     if not obuild.reference_available():
         raise SystemExit(f"reference source not found at {obuild.REFERENCE_SRC}")
@@ -260,6 +293,9 @@ def main():
     kat_prop("periodic2d", srn.configs.bulk2d(nx=32, nz=24, iters=1), steps=12, seed=201)
     kat_prop("dirichlet2d", srn.configs.film2d(nx=24, nz=16, ns=64, iters=1), steps=12, seed=202)
     kat_prop("periodic3d", srn.configs.blend3d(n=8, ns=24, iters=1), steps=6, seed=203)
+    # odd interval count (the dropped point stop-1), an even one, and a block starting mid-chain
+    kat_density("2d", srn.configs.bulk2d(nx=16, nz=12, iters=1), ns=21, blocks=[(0, 20), (0, 9), (9, 20), (3, 14)],
+                seed=204)
 
 
 if __name__ == "__main__":

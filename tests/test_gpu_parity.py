@@ -216,3 +216,18 @@ def test_film3d_mask_vs_oracle(srn, oracle_mod):
     scale = np.maximum(np.abs(ophi).max(axis=1, keepdims=True), 1e-300)
     assert np.all(np.abs(phi - ophi) <= PHI_RTOL * scale + 1e-15)
     o.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_density_unit_matches_funDensity(srn, precision):
+    """scft_density (the kernel the iteration uses) against the reference's
+    funMultiplyQs + funDensity on the same propagators (kat_density_2d)."""
+    from conftest import load_golden
+    g = load_golden("kat_density_2d")
+    nx, ny, nz = (int(v) for v in g["grid"])
+    S = srn.configs.bulk2d(nx=nx, nz=nz, iters=1)
+    tol = 1e-13 if precision == "fp64" else 2e-7
+    with srn.Solver(S, precision=precision) as sv:
+        for (start, stop), phi in zip(g["blocks"], g["phi"]):
+            got = sv.density(g["qf"], g["qb"], int(start), int(stop), float(g["Q"]))
+            np.testing.assert_allclose(got, phi, rtol=tol, atol=0)

@@ -86,3 +86,18 @@ def test_oracle_surface_layout_matches_library(srn, oracle_mod):
     from importlib import import_module
     L = import_module("stimuli-responsive-nanodroplets_gb300._lib")
     assert oracle_mod.lib().orc_surface_size() == ctypes.sizeof(L.CSurface)
+
+
+def test_oracle_density_matches_funDensity(srn, oracle_mod):
+    """funMultiplyQs + funDensity of the reference (shared build, kat_density_2d)
+    against the oracle's restatement, including the point stop-1 that an odd
+    interval count leaves out."""
+    from conftest import load_golden
+    g = load_golden("kat_density_2d")
+    nx, ny, nz = (int(v) for v in g["grid"])
+    S = srn.configs.bulk2d(nx=nx, nz=nz, iters=1)
+    o = oracle_mod.Oracle(S)
+    for (start, stop), phi in zip(g["blocks"], g["phi"]):
+        got = o.density(g["qf"], g["qb"], int(start), int(stop), float(g["Q"]))
+        np.testing.assert_allclose(got, phi, rtol=1e-14, atol=0)
+    o.close()
