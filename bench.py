@@ -443,8 +443,9 @@ def workload_config(args, surfaces):
     s = surfaces[0]
     nx, ny, nz = s.grid()
     start = "seeded droplet start" if s.MASK else "seeded w-noise start"
+    sweep = "seeded chi N matrices" if args.workload == "blend3d" else "chi_AB x chi_AC sweep"
     return {"workload": f"{args.workload} {nx}x{ny}x{nz} NS={s.NS} MASK={s.MASK}, {len(surfaces)} instances "
-                        f"(chi_AB x chi_AC sweep), {start}",
+                        f"({sweep}), {start}",
             "instances_per_gpu": len(surfaces), "grid": [nx, ny, nz], "ns": s.NS, "mask": s.MASK,
             "l2": "working set larger than L2 (propagators of all instances)",
             "parallelism": "replicas (one batch per GPU)"}
