@@ -329,7 +329,8 @@ def _pass_stats(serve, done, wall, classes):
     return st
 
 
-def measure_serving(srn, n_requests: int, rate_hz: float, rms_tol: float, max_iter: int, device: int):
+def measure_serving(srn, n_requests: int, rate_hz: float, rms_tol: float, max_iter: int, device: int,
+                    winners: int = 4):
     """Poisson streams of phase-diagram solve requests over 3 planes x 24x24
     (chi_AB N, chi_AC N) points: 70% 2D 192x96 thin film (one in five of those in
     the plain FP64 form), 30% 3D 64^3 bulk blend, NS = 100; slots from a
@@ -392,16 +393,76 @@ def measure_serving(srn, n_requests: int, rate_hz: float, rms_tol: float, max_it
         reqs2.append(serve.Request(rid=1000 + r, cls=cls, surface=s, w14=c.fields,
                                    mask3=cfg.substrate_mask(s) if cls == "film2d" else None, precision=c.precision,
                                    arrival=t, key=(cls, pl, i, j), seed=(r, 9, 7)))
-    server.keep_fields = False
     t0 = time.perf_counter()
     second = server.run(reqs2)
     wall2 = time.perf_counter() - t0
-    server.close()
     st = _pass_stats(serve, second, wall2, slots)
     st.update({"pass": "neighbour-seeded (second pass)", "rate_hz": rate_hz, "rms_tol": rms_tol,
                "max_iter": max_iter, "slots": {f"{k[0]}/{k[1]}": v for k, v in slots.items()},
                "first_pass": _pass_stats(serve, first, wall1, slots)})
+    if winners > 1:
+        st["winners"] = winner_check(serve, server, second, surface, cfg, winners)
+    server.close()
     return st
+
+
+def winner_check(serve, server, done, surface, cfg, k: int) -> dict:
+    """Lowest-F winners of the FP32 form against the plain FP64 form, after the
+    serving passes (not part of their timing). Up to k converged FP32 thin-film
+    results of the second pass give k points and k structures; every structure
+    is relaxed at every other point in FP32 (the phase-diagram trial), then every
+    converged FP32 structure is relaxed again in the plain FP64 form from its
+    FP32 field, and each point's lowest-F structure is compared between the two
+    forms. Structures whose FP32 free energies lie within 1e-6 relative of the
+    winner's are the same structure to FP32 accuracy and count as ties."""
+    films = [c for c in sorted(done, key=lambda c: c.rid)
+             if c.cls == "film2d" and c.precision == "fp32" and c.converged and c.fields is not None][:k]
+    k = len(films)
+    if k < 2:
+        return {"points": k, "compared": 0, "note": "fewer than two converged FP32 thin-film results"}
+    surf = [surface(c.key[0], c.key[1], c.key[2], c.key[3]) for c in films]
+    mk = [cfg.substrate_mask(s) for s in surf]
+    rid = 100000
+    reqs = []
+    for a in range(k):
+        for b in range(k):
+            if a != b:
+                rid += 1
+                reqs.append(serve.Request(rid=rid, cls="film2d", surface=surf[a], w14=films[b].fields, mask3=mk[a],
+                                          precision="fp32", key=(a, b), seed=(a, b, 3)))
+    keep = server.keep_fields
+    server.keep_fields = True
+    try:
+        F32 = {(a, a): (films[a].free_energy, films[a].converged, films[a].fields) for a in range(k)}
+        for c in server.run(reqs, realtime=False):
+            F32[c.key] = (c.free_energy, c.converged, c.fields)
+        reqs64 = []
+        for (a, b), (f, conv, w) in F32.items():
+            if conv and np.isfinite(f):
+                rid += 1
+                reqs64.append(serve.Request(rid=rid, cls="film2d", surface=surf[a], w14=w, mask3=mk[a],
+                                            precision="fp64", key=(a, b), seed=(a, b, 5)))
+        F64 = {c.key: (c.free_energy, c.converged) for c in server.run(reqs64, realtime=False)}
+    finally:
+        server.keep_fields = keep
+    compared = agree = ties = 0
+    max_rel = 0.0
+    for a in range(k):
+        cand = [b for b in range(k) if (a, b) in F64 and F64[(a, b)][1]]
+        for b in cand:
+            max_rel = max(max_rel, abs(F32[(a, b)][0] - F64[(a, b)][0]) / abs(F64[(a, b)][0]))
+        if len(cand) < 2:
+            continue
+        compared += 1
+        w32 = min(cand, key=lambda b: F32[(a, b)][0])
+        w64 = min(cand, key=lambda b: F64[(a, b)][0])
+        if w32 == w64:
+            agree += 1
+        elif abs(F32[(a, w64)][0] - F32[(a, w32)][0]) <= 1e-6 * abs(F32[(a, w32)][0]):
+            ties += 1
+    return {"points": k, "fp32_trials": len(reqs), "fp64_relaxations": len(reqs64), "compared": compared,
+            "same_winner": agree, "ties_within_1e-6": ties, "different_winner": compared - agree - ties,
+            "max_rel_dF_fp32_vs_fp64": max_rel}
 
 
 def cpu_sample(surfaces, threads: int, iters: int):
@@ -509,6 +570,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=4.0, help="mean arrivals per second")
     ap.add_argument("--serve-tol", type=float, default=1e-3)
     ap.add_argument("--serve-max-iter", type=int, default=3000)
+    ap.add_argument("--serve-winners", type=int, default=4,
+                    help="points of the FP32-vs-FP64 lowest-F winner check after serving (0: skip)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one iteration of one form only (for ncu captures); prints no bench line")
     args = ap.parse_args()
@@ -591,7 +654,7 @@ def main():
                                       local, sync)
     if args.serve_requests > 0:
         line["serving"] = measure_serving(srn, args.serve_requests, args.serve_rate, args.serve_tol,
-                                          args.serve_max_iter, local)
+                                          args.serve_max_iter, local, args.serve_winners)
     if rank == 0 and not args.no_cpu:
         threads = args.cpu_threads or os.cpu_count() or 1
         rate, wall = cpu_sample(surfaces, threads, args.cpu_iters)
