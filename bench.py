@@ -410,11 +410,13 @@ def winner_check(serve, server, done, surface, cfg, k: int) -> dict:
     """Lowest-F winners of the FP32 form against the plain FP64 form, after the
     serving passes (not part of their timing). Up to k converged FP32 thin-film
     results of the second pass give k points and k structures; every structure
-    is relaxed at every other point in FP32 (the phase-diagram trial), then every
-    converged FP32 structure is relaxed again in the plain FP64 form from its
-    FP32 field, and each point's lowest-F structure is compared between the two
-    forms. Structures whose FP32 free energies lie within 1e-6 relative of the
-    winner's are the same structure to FP32 accuracy and count as ties."""
+    is relaxed at every other point in FP32 (the phase-diagram trial, same
+    tolerance and iteration cap as the stream). Both forms then evaluate the
+    free energy of every converged structure on the same fields (one iteration
+    each: the reference's F uses the fields before the update), and each
+    point's lowest-F structure is compared between the two forms. Structures
+    whose FP32 free energies lie within 1e-6 relative of the winner's are the
+    same structure to FP32 accuracy and count as ties."""
     films = [c for c in sorted(done, key=lambda c: c.rid)
              if c.cls == "film2d" and c.precision == "fp32" and c.converged and c.fields is not None][:k]
     k = len(films)
@@ -433,34 +435,36 @@ def winner_check(serve, server, done, surface, cfg, k: int) -> dict:
     keep = server.keep_fields
     server.keep_fields = True
     try:
-        F32 = {(a, a): (films[a].free_energy, films[a].converged, films[a].fields) for a in range(k)}
+        relaxed = {(a, a): (films[a].converged, films[a].fields) for a in range(k)}
         for c in server.run(reqs, realtime=False):
-            F32[c.key] = (c.free_energy, c.converged, c.fields)
-        reqs64 = []
-        for (a, b), (f, conv, w) in F32.items():
-            if conv and np.isfinite(f):
-                rid += 1
-                reqs64.append(serve.Request(rid=rid, cls="film2d", surface=surf[a], w14=w, mask3=mk[a],
-                                            precision="fp64", key=(a, b), seed=(a, b, 5)))
-        F64 = {c.key: (c.free_energy, c.converged) for c in server.run(reqs64, realtime=False)}
+            relaxed[c.key] = (c.converged and np.isfinite(c.free_energy), c.fields)
     finally:
         server.keep_fields = keep
+    keys = sorted(key for key, (conv, _) in relaxed.items() if conv)
+    Solver = importlib.import_module(PKG).Solver
+    F = {}
+    for prec in ("fp32", "fp64"):
+        with Solver([surf[a] for a, _ in keys], precision=prec) as sv:
+            for n, (a, b) in enumerate(keys):
+                sv.set_fields(relaxed[(a, b)][1], n)
+                sv.set_masks(mk[a], n)
+                sv.set_iteration(1, n)
+            out = sv.iterate(1)[0]
+            F[prec] = {key: out[n].free_energy for n, key in enumerate(keys)}
     compared = agree = ties = 0
-    max_rel = 0.0
+    max_rel = max(abs(F["fp32"][key] - F["fp64"][key]) / abs(F["fp64"][key]) for key in keys)
     for a in range(k):
-        cand = [b for b in range(k) if (a, b) in F64 and F64[(a, b)][1]]
-        for b in cand:
-            max_rel = max(max_rel, abs(F32[(a, b)][0] - F64[(a, b)][0]) / abs(F64[(a, b)][0]))
+        cand = [b for (a2, b) in keys if a2 == a]
         if len(cand) < 2:
             continue
         compared += 1
-        w32 = min(cand, key=lambda b: F32[(a, b)][0])
-        w64 = min(cand, key=lambda b: F64[(a, b)][0])
+        w32 = min(cand, key=lambda b: F["fp32"][(a, b)])
+        w64 = min(cand, key=lambda b: F["fp64"][(a, b)])
         if w32 == w64:
             agree += 1
-        elif abs(F32[(a, w64)][0] - F32[(a, w32)][0]) <= 1e-6 * abs(F32[(a, w32)][0]):
+        elif abs(F["fp32"][(a, w64)] - F["fp32"][(a, w32)]) <= 1e-6 * abs(F["fp32"][(a, w32)]):
             ties += 1
-    return {"points": k, "fp32_trials": len(reqs), "fp64_relaxations": len(reqs64), "compared": compared,
+    return {"points": k, "fp32_trials": len(reqs), "structures_evaluated": len(keys), "compared": compared,
             "same_winner": agree, "ties_within_1e-6": ties, "different_winner": compared - agree - ties,
             "max_rel_dF_fp32_vs_fp64": max_rel}
 

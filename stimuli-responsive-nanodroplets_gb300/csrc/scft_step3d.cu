@@ -6,8 +6,10 @@
  *
  * The 1 MB slice of a chain lives in the shared memory of an 8-CTA cluster for
  * the chain's whole contour loop, as 8 planes of 64 rows of 64 z values per CTA
- * (row pitch 65 floats, plane pitch 64*65+4, so the row and column walks below
- * are free of bank conflicts). Two distributions alternate:
+ * (row pitch 68 floats: every row starts on a 16-byte boundary, so rows move as
+ * 128-bit words, and a quarter-warp walking 8 rows side by side in 128-bit
+ * steps touches 8 different bank groups; column walks are conflict-free for
+ * any pitch). Two distributions alternate:
  *   D1: CTA r holds x in [8r, 8r+8) as planes, y as rows;
  *   D2: CTA r holds y in [8r, 8r+8) as planes, x as rows.
  * The factor is separable, real and even per axis, so each axis is applied as
@@ -17,8 +19,8 @@
  * distributions, so a step starting in D1 applies z and y, moves to D2 (one
  * all-to-all through distributed shared memory), applies x, and the next step
  * does z and x, moves back and applies y. Per step: one exchange (each CTA
- * pulls 7/8 of its new contents into registers, a cluster barrier, writes them
- * to its own planes), two cluster barriers, and to HBM only q_{s+1} (for the
+ * pulls 7/8 of its new contents into registers as 128-bit words, a cluster
+ * barrier, writes them to its own planes), two cluster barriers, and to HBM only q_{s+1} (for the
  * densities) with b read once. All control flow is uniform over the cluster
  * (one chain per cluster), and a last cluster barrier keeps every CTA's shared
  * memory alive until no other CTA can address it.
@@ -35,8 +37,9 @@ namespace {
 constexpr int N3 = 64;            /* points per axis */
 constexpr int CL = 8;             /* CTAs per cluster */
 constexpr int PL = N3 / CL;       /* x planes per CTA */
-constexpr int RP = N3 + 1;        /* row pitch (floats) */
-constexpr int PP = N3 * RP + 4;   /* plane pitch (floats) */
+constexpr int RP = N3 + 4;        /* row pitch (floats), a multiple of 4 */
+constexpr int PP = N3 * RP;       /* plane pitch (floats) */
+constexpr int RP4 = RP / 4, PP4 = PP / 4; /* the same in float4 */
 constexpr int NT = 256;           /* threads per CTA: 8 warps x 32 lanes */
 constexpr int UB = 16;            /* float4 loads in flight per thread in the pointwise phases */
 
@@ -163,16 +166,27 @@ __device__ __forceinline__ void fft64(C2 *v)
     }
 }
 
-/* real circulant along one local axis for two packed lines: x0[i*st], x1[i*st].
- * The inverse transform is the forward one on the conjugate (conj(F(conj Y))),
- * so one copy of the 64-point FFT serves both directions, and the function is
- * kept out of line: the three call sites per contour step share one copy of
- * the code, which keeps the kernel inside the instruction cache. */
-__device__ __forceinline__ void conv_line(float *x0, float *x1, int st, const float *E)
+/* real circulant along one local axis for two packed lines: x0[i*ST], x1[i*ST]
+ * (ST = 1: the lines are rows and move as 128-bit words). The inverse transform
+ * is the forward one on the conjugate (conj(F(conj Y))), so one copy of the
+ * 64-point FFT code, run as a loop of two passes, serves both directions. */
+template <int ST>
+__device__ __forceinline__ void conv_line(float *x0, float *x1, const float *E)
 {
     C2 v[64];
+    if constexpr (ST == 1) {
 #pragma unroll
-    for (int i = 0; i < 64; ++i) v[i] = C2{x0[i * st], x1[i * st]};
+        for (int i = 0; i < 16; ++i) {
+            const float4 a = reinterpret_cast<const float4 *>(x0)[i], b = reinterpret_cast<const float4 *>(x1)[i];
+            v[4 * i] = C2{a.x, b.x};
+            v[4 * i + 1] = C2{a.y, b.y};
+            v[4 * i + 2] = C2{a.z, b.z};
+            v[4 * i + 3] = C2{a.w, b.w};
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = C2{x0[i * ST], x1[i * ST]};
+    }
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         fft64<false>(v);
@@ -184,10 +198,19 @@ __device__ __forceinline__ void conv_line(float *x0, float *x1, int st, const fl
             }
         }
     }
+    if constexpr (ST == 1) {
 #pragma unroll
-    for (int i = 0; i < 64; ++i) {
-        x0[i * st] = v[i].x;
-        x1[i * st] = -v[i].y;
+        for (int i = 0; i < 16; ++i) {
+            reinterpret_cast<float4 *>(x0)[i] = make_float4(v[4 * i].x, v[4 * i + 1].x, v[4 * i + 2].x, v[4 * i + 3].x);
+            reinterpret_cast<float4 *>(x1)[i] =
+                make_float4(-v[4 * i].y, -v[4 * i + 1].y, -v[4 * i + 2].y, -v[4 * i + 3].y);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+            x0[i * ST] = v[i].x;
+            x1[i * ST] = -v[i].y;
+        }
     }
 }
 
@@ -238,11 +261,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(St
 #pragma unroll
             for (int u = 0; u < UB; ++u) {
                 const int e = 4 * (base + u * NT);
-                float *dq = Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63);
-                dq[0] = qv[u].x * bv[u].x;
-                dq[1] = qv[u].y * bv[u].y;
-                dq[2] = qv[u].z * bv[u].z;
-                dq[3] = qv[u].w * bv[u].w;
+                float4 *dq = reinterpret_cast<float4 *>(Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63));
+                *dq = make_float4(qv[u].x * bv[u].x, qv[u].y * bv[u].y, qv[u].z * bv[u].z, qv[u].w * bv[u].w);
             }
         }
     }
@@ -253,30 +273,33 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(St
         /* z lines: plane `warp`, rows lane and lane+32 */
         {
             float *r0 = Q + warp * PP + lane * RP;
-            conv_line(r0, r0 + 32 * RP, 1, E + 2 * N3);
+            conv_line<1>(r0, r0 + 32 * RP, E + 2 * N3);
         }
         __syncthreads();
         /* row lines (y in D1, x in D2): plane `warp`, columns lane and lane+32 */
         {
             float *c0 = Q + warp * PP + lane;
-            conv_line(c0, c0 + 32, RP, E + (d == 0 ? N3 : 0));
+            conv_line<RP>(c0, c0 + 32, E + (d == 0 ? N3 : 0));
         }
         cl.sync(); /* every CTA's planes are final for this half of the step */
         /* exchange: (CTA c, plane p, row 8 rank + j) -> (this CTA, plane j, row 8 c + p); warp w
-         * pulls everything this CTA receives from CTA w, 128 values per thread in registers */
+         * pulls everything this CTA receives from CTA w: 64 rows of 16 128-bit words, two rows
+         * per warp-wide load, 32 words per thread in registers */
         {
-            const float *src = cl.map_shared_rank(Q, warp);
-            float v[128];
+            const float4 *src = reinterpret_cast<const float4 *>(cl.map_shared_rank(Q, warp));
+            float4 *dst = reinterpret_cast<float4 *>(Q);
+            const int f = lane & 15, half = lane >> 4;
+            float4 v[32];
 #pragma unroll
-            for (int i = 0; i < 128; ++i) {
-                const int p = i >> 4, j = (i >> 1) & 7, zh = i & 1;
-                v[i] = src[p * PP + (PL * rank + j) * RP + 32 * zh + lane];
+            for (int it = 0; it < 32; ++it) {
+                const int ri = 2 * it + half, p = ri >> 3, j = ri & 7;
+                v[it] = src[p * PP4 + (PL * rank + j) * RP4 + f];
             }
             cl.sync(); /* every CTA has its inputs: planes may be overwritten */
 #pragma unroll
-            for (int i = 0; i < 128; ++i) {
-                const int p = i >> 4, j = (i >> 1) & 7, zh = i & 1;
-                Q[j * PP + (PL * warp + p) * RP + 32 * zh + lane] = v[i];
+            for (int it = 0; it < 32; ++it) {
+                const int ri = 2 * it + half, p = ri >> 3, j = ri & 7;
+                dst[j * PP4 + (PL * warp + p) * RP4 + f] = v[it];
             }
         }
         d ^= 1;
@@ -284,7 +307,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(St
         /* the remaining axis along the rows of the new distribution */
         {
             float *c0 = Q + warp * PP + lane;
-            conv_line(c0, c0 + 32, RP, E + (d == 0 ? N3 : 0));
+            conv_line<RP>(c0, c0 + 32, E + (d == 0 ? N3 : 0));
         }
         __syncthreads();
         /* q_{s+1} = b_s . y to HBM; the next step starts from b_{s+1} . q_{s+1} */
@@ -305,15 +328,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_chain3d(St
                 for (int u = 0; u < UB; ++u) {
                     const int e = 4 * (base + u * NT);
                     const long g = g_index(e, rank, d);
-                    float *dq = Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63);
-                    const float4 o = {dq[0] * bv[u].x, dq[1] * bv[u].y, dq[2] * bv[u].z, dq[3] * bv[u].w};
+                    float4 *dq = reinterpret_cast<float4 *>(Q + (e >> 12) * PP + ((e >> 6) & 63) * RP + (e & 63));
+                    const float4 y = *dq;
+                    const float4 o = {y.x * bv[u].x, y.y * bv[u].y, y.z * bv[u].z, y.w * bv[u].w};
                     *reinterpret_cast<float4 *>(qn + g) = o;
-                    if (more) {
-                        dq[0] = o.x * nv[u].x;
-                        dq[1] = o.y * nv[u].y;
-                        dq[2] = o.z * nv[u].z;
-                        dq[3] = o.w * nv[u].w;
-                    }
+                    if (more) *dq = make_float4(o.x * nv[u].x, o.y * nv[u].y, o.z * nv[u].z, o.w * nv[u].w);
                 }
             }
         }
