@@ -389,6 +389,9 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
 
     const int tid = threadIdx.x;
     const P *qs = reinterpret_cast<const P *>(cd.q) + (long)a.s * a.sstride;
+    /* phase A folded into the store phase: every thread owns whole work items */
+    constexpr bool FUSE_A = sizeof(P) == 4 && (N2 * NZ2) % NX == 0;
+    constexpr int ITEMS = (N2 * NZ2) / NX;
 
     /* operators and tables, once per chain (16-byte asynchronous copies) */
     {
@@ -435,7 +438,9 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     const P *bz = reinterpret_cast<const P *>(s < cd.seg_end ? cd.b0 : cd.b1);
     const P *bnext = reinterpret_cast<const P *>(s + 1 < cd.seg_end ? cd.b0 : cd.b1);
     P *qn = reinterpret_cast<P *>(cd.q) + (long)(s + 1) * a.sstride;
-    /* A: DFT_N1 over rows N2*n1 + n2 of b . q_s, twiddle, back to rows N2*k1 + n2 */
+    /* A: DFT_N1 over rows N2*n1 + n2 of b . q_s, twiddle, back to rows N2*k1 + n2
+     * (after the first step this runs inside the previous step's store phase) */
+    if (!FUSE_A || s == a.s) {
     for (int w = tid; w < N2 * NZ2; w += NX) {
         const int n2 = w / NZ2, c = w - n2 * NZ2;
         Cx<P> v[N1];
@@ -448,6 +453,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
     }
     __syncthreads();
+    }
     /* B: DFT_N2 over rows N2*k1 .. N2*k1+N2-1, E(k)/N, inverse, conjugate twiddle */
     for (int w = tid; w < N1 * NZ2; w += NX) {
         const int k1 = w / NZ2, c = w - k1 * NZ2;
@@ -586,8 +592,44 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     /* q_{s+1} = b . y to HBM for the densities; the next step's input
      * b_next . q_{s+1} stays in shared memory (b_next differs from b only at the
      * diblock junction), so b is read once per step. Each thread issues all of
-     * its b loads before using any: L2 latency is paid once per step. */
-    {
+     * its b loads before using any: L2 latency is paid once per step. Unless
+     * this is the last step, each thread walks the columns of its phase-A work
+     * items, so the next step's phase A runs on the values in registers. */
+    if (FUSE_A && s + 1 < s_end) {
+        const T2 *b2p = reinterpret_cast<const T2 *>(bz);
+        const T2 *n2p = reinterpret_cast<const T2 *>(bnext);
+        const bool same_b = (bnext == bz);
+        T2 bb[ITEMS * N1];
+#pragma unroll
+        for (int it = 0; it < ITEMS; ++it) {
+            const int w = tid + it * NX, n2 = w / NZ2, c = w - n2 * NZ2;
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) bb[it * N1 + n1] = b2p[(N2 * n1 + n2) * NZ2 + c];
+        }
+#pragma unroll
+        for (int it = 0; it < ITEMS; ++it) {
+            const int w = tid + it * NX, n2 = w / NZ2, c = w - n2 * NZ2;
+            Cx<P> v[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) {
+                const int e = (N2 * n1 + n2) * NZ2 + c;
+                const T2 y = reinterpret_cast<const T2 *>(X)[(N2 * n1 + n2) * ZP2 + c];
+                const T2 bv = bb[it * N1 + n1];
+                T2 o;
+                o.x = y.x * bv.x;
+                o.y = y.y * bv.y;
+                reinterpret_cast<T2 *>(qn)[e] = o;
+                const T2 nb = same_b ? bv : n2p[e];
+                v[n1].x = o.x * nb.x;
+                v[n1].y = o.y * nb.y;
+            }
+            Dft<P, N1, false>::run(v);
+#pragma unroll
+            for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], TW[n2 * N1 + k1]);
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
+        }
+    } else {
         constexpr int PER = NZ2; /* pairs per thread */
         constexpr int BATCH = PER;
         const T2 *b2p = reinterpret_cast<const T2 *>(bz);
