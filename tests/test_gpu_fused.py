@@ -26,7 +26,8 @@ def test_fused_propagate_matches_funPDESolver(tag, srn):
 
 
 @pytest.mark.parametrize("shape,mask", [((192, 96), 1), ((192, 128), 1), ((128, 96), 1), ((96, 64), 1),
-                                        ((64, 64), 0), ((64, 32), 0), ((32, 32), 0)])
+                                        ((64, 64), 0), ((64, 32), 0), ((32, 32), 0), ((32, 24), 0),
+                                        ((32, 16), 1), ((24, 16), 0), ((16, 16), 0)])
 def test_fused_matches_axis_passes(shape, mask, srn):
     nx, nz = shape
     if mask:
