@@ -281,7 +281,8 @@ typedef struct scft_timing {
     long kernel_launches;
     int fused_chain;   /* contour steps run in one persistent launch: 1 the fused 2D chain kernel,
                           2 the 64^3 cluster kernel; 0 per-axis passes */
-    int pad;
+    int threads_per_line; /* fused 2D kernel: 2 when a batch of at most one chain per SM gives each
+                             line two threads (bit-identical results), else 1 */
 } scft_timing;
 int scft_enable_timing(scft_ctx *ctx, int on);
 int scft_get_timing(const scft_ctx *ctx, scft_timing *t);

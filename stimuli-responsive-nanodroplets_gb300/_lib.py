@@ -100,7 +100,7 @@ class CBatchResult(C.Structure):
 
 class CTiming(C.Structure):
     _fields_ = [("total_ms", D), ("prop_ms", D), ("prop_launches", C.c_long), ("kernel_launches", C.c_long),
-                ("fused_chain", C.c_int), ("pad", C.c_int)]
+                ("fused_chain", C.c_int), ("threads_per_line", C.c_int)]
 
 
 _lib = None

@@ -91,6 +91,7 @@ struct scft_ctx {
     std::vector<ChainSpec> cs0; /* instance 0's chains: the composition every instance shares */
     /* fused contour loops: 2D (scft_step2d.cu), 64^3 clusters (scft_step3d.cu) */
     int fused2d = 0;
+    int wide2d = 0; /* fused 2D loop with two threads per line (batches of at most one chain per SM) */
     int fused3d = 0;
     int *order = nullptr; /* chain indices, longest first */
     /* device noise replay (SCFT_NOISE_DRAND48) */
@@ -354,8 +355,11 @@ static int build_fused2d(scft_ctx *c)
     }
     Step2DArgs a;
     memset(&a, 0, sizeof(a));
-    CK(scft_launch_step2d(c->opt.precision, nx, d0.nz, a, 0, c->stream, 1));
+    CK(scft_launch_step2d(c->opt.precision, nx, d0.nz, a, 0, c->stream, 1, 0));
     c->fused2d = 1;
+    /* a batch with at most one chain per SM runs one CTA per SM either way: twice
+     * the threads per chain shortens each step, with bit-identical results */
+    c->wide2d = scft_step2d_wide(c->opt.precision, nx, d0.nz) && (long)c->B * c->nchains <= c->sms;
     return SCFT_OK;
 }
 /* Operator tables of one grid axis (pass slot ai) for one operator set. */
@@ -1198,7 +1202,7 @@ static int launch_steps(scft_ctx *c, const ChainDesc *chains, int nchains_total,
         if (c->fused3d)
             CK(scft_launch_step3d(a, nchains_total, c->stream, 0));
         else
-            CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0));
+            CK(scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, nchains_total, c->stream, 0, c->wide2d));
         return SCFT_OK;
     }
     const int npass = (int)c->axes.size();
@@ -1672,6 +1676,7 @@ extern "C" int scft_get_timing(const scft_ctx *c, scft_timing *t)
     if (!c || !t) return SCFT_ERR_PARAM;
     *t = c->last_timing;
     t->fused_chain = c->fused2d ? 1 : (c->fused3d ? 2 : 0);
+    t->threads_per_line = c->fused2d && c->wide2d ? 2 : 1;
     return SCFT_OK;
 }
 

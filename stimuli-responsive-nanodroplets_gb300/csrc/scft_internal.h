@@ -188,7 +188,9 @@ size_t scft_step3d_smem(int prec, int nx, int ny, int nz);
 cudaError_t scft_launch_step3d(const Step2DArgs &a, int nchains, cudaStream_t st, int configure);
 int scft_step2d_n1(int nx);
 cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
-                               int configure);
+                               int configure, int wide);
+/* 1 if (nx, nz) has the two-threads-per-line form of the fused 2D loop */
+int scft_step2d_wide(int prec, int nx, int nz);
 
 /* Internal hooks of scft_ctx.cu for the allocation-free propagator entry point. */
 int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st,

@@ -281,12 +281,20 @@ struct Dft<P, 16, INV> {
 /* z operator, two lines per thread pair: thread (p, h) holds the k-half h of
  * the sums and differences of lines 2p and 2p+1, so every operator value it
  * loads feeds both lines; the two partial sums of an output meet through one
- * shuffle, and each thread finishes the outputs of its own half. */
-template <int NX, int NZ>
-__device__ __forceinline__ void z_split2(float *X, const float *KA, const float *KB, int tid)
+ * shuffle, and each thread finishes the outputs of its own half. With TM > 1
+ * thread groups (TM * NX threads), group g computes the outputs jo in
+ * [g KH/TM, (g+1) KH/TM) of every line pair with the same arithmetic, so the
+ * results do not depend on TM. */
+template <int NX, int NZ, int TM = 1>
+__device__ __forceinline__ void z_split2(float *X, const float *KA, const float *KB, int t)
 {
     constexpr int ZP = NZ + 2, H = NZ / 2, KH = H / 2, KQ = KH / 4;
-    constexpr unsigned MASK = (NX % 32 == 0) ? 0xffffffffu : ((1u << (NX % 32)) - 1u);
+    static_assert(KH % TM == 0, "output groups must split the half rows evenly");
+    /* the lanes of this warp that exist in a block of NX * TM threads */
+    constexpr int NT = NX * TM;
+    const int lanes = NT - (t & ~31);
+    const unsigned MASK = (NT % 32 == 0 || lanes >= 32) ? 0xffffffffu : ((1u << lanes) - 1u);
+    const int tid = TM == 1 ? t : t % NX, g = TM == 1 ? 0 : t / NX;
     const int p = tid >> 1, h = tid & 1;
     float *r0 = X + (2 * p) * ZP;
     float *r1 = r0 + ZP;
@@ -304,7 +312,8 @@ __device__ __forceinline__ void z_split2(float *X, const float *KA, const float 
         u1[j] = pack2(a1.x + m1.y, a1.y + m1.x);
         v1[j] = pack2(a1.x - m1.y, a1.y - m1.x);
     }
-    for (int jo = 0; jo < KH; ++jo) {
+    if constexpr (TM > 1) __syncthreads(); /* every group has its lines before any output lands */
+    for (int jo = g * (KH / TM); jo < (g + 1) * (KH / TM); ++jo) {
         unsigned long long s00 = 0ull, s01 = 0ull, s10 = 0ull, s11 = 0ull; /* s[row][line] */
         unsigned long long d00 = 0ull, d01 = 0ull, d10 = 0ull, d11 = 0ull;
         const float4 *a0p = reinterpret_cast<const float4 *>(KA + jo * H + k0);
@@ -362,9 +371,10 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
  * the slice stays in shared memory from step to step (q_{s+1} is written to
  * HBM for the densities and kept for the next step), the operator tables are
  * loaded once. Chains are taken longest first through a.order. */
-template <typename P, int NX, int NZ, int N1, int N2>
-__global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
+template <typename P, int NX, int NZ, int N1, int N2, int TM>
+__global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
 {
+    constexpr int T = NX * TM; /* threads: TM per line */
     static_assert(N1 * N2 == NX, "NX = N1 * N2");
     static_assert(NZ % 4 == 0, "NZ must be a multiple of 4");
     constexpr int ZP = NZ + 2;  /* row pitch (elements) */
@@ -391,24 +401,25 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     const P *qs = reinterpret_cast<const P *>(cd.q) + (long)a.s * a.sstride;
     /* phase A folded into the store phase: every thread owns whole work items */
     constexpr bool FUSE_A = sizeof(P) == 4 && (N2 * NZ2) % NX == 0;
-    constexpr int ITEMS = (N2 * NZ2) / NX;
+    constexpr int ITEMS = (N2 * NZ2 + T - 1) / T;
+    constexpr bool ITEMS_EVEN = (N2 * NZ2) % T == 0;
 
     /* operators and tables, once per chain (16-byte asynchronous copies) */
     {
         constexpr int VP = 16 / sizeof(P);
         const P *gA = reinterpret_cast<const P *>(cd.ops->kz);
-        for (int e = tid; e < H * H / VP; e += NX) {
+        for (int e = tid; e < H * H / VP; e += T) {
             cp_async16(KA + e * VP, gA + e * VP);
             cp_async16(KB + e * VP, gA + H * H + e * VP);
         }
         const P *gT = reinterpret_cast<const P *>(cd.ops->twx);
-        for (int e = tid; e < 2 * NX / VP; e += NX) cp_async16(reinterpret_cast<P *>(TW) + e * VP, gT + e * VP);
+        for (int e = tid; e < 2 * NX / VP; e += T) cp_async16(reinterpret_cast<P *>(TW) + e * VP, gT + e * VP);
         const P *gE = reinterpret_cast<const P *>(cd.ops->ex);
-        for (int e = tid; e < NX / VP; e += NX) cp_async16(EX + e * VP, gE + e * VP);
+        for (int e = tid; e < NX / VP; e += T) cp_async16(EX + e * VP, gE + e * VP);
     }
     /* load q_s into the padded rows with asynchronous 2-element copies: every
      * copy of the slice is in flight at once and none holds a register */
-    for (int e = tid; e < NX * NZ2; e += NX) {
+    for (int e = tid; e < NX * NZ2; e += T) {
         const int x = e / NZ2, c = e - x * NZ2;
         const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<T2 *>(X) + x * ZP2 + c);
         if (sizeof(T2) == 8)
@@ -424,7 +435,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     {
         const P *b_first = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
 #pragma unroll 4
-        for (int e = tid; e < NX * NZ2; e += NX) {
+        for (int e = tid; e < NX * NZ2; e += T) {
             const int x = e / NZ2, c = e - x * NZ2;
             const T2 b2 = reinterpret_cast<const T2 *>(b_first)[e];
             T2 &v = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
@@ -441,7 +452,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     /* A: DFT_N1 over rows N2*n1 + n2 of b . q_s, twiddle, back to rows N2*k1 + n2
      * (after the first step this runs inside the previous step's store phase) */
     if (!FUSE_A || s == a.s) {
-    for (int w = tid; w < N2 * NZ2; w += NX) {
+    for (int w = tid; w < N2 * NZ2; w += T) {
         const int n2 = w / NZ2, c = w - n2 * NZ2;
         Cx<P> v[N1];
 #pragma unroll
@@ -455,7 +466,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     __syncthreads();
     }
     /* B: DFT_N2 over rows N2*k1 .. N2*k1+N2-1, E(k)/N, inverse, conjugate twiddle */
-    for (int w = tid; w < N1 * NZ2; w += NX) {
+    for (int w = tid; w < N1 * NZ2; w += T) {
         const int k1 = w / NZ2, c = w - k1 * NZ2;
         Cx<P> u[N2];
 #pragma unroll
@@ -482,7 +493,7 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     }
     __syncthreads();
     /* C: inverse DFT_N1 back to natural rows */
-    for (int w = tid; w < N2 * NZ2; w += NX) {
+    for (int w = tid; w < N2 * NZ2; w += T) {
         const int n2 = w / NZ2, c = w - n2 * NZ2;
         Cx<P> v[N1];
 #pragma unroll
@@ -494,8 +505,10 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
     __syncthreads();
 
     /* z: one row per thread, y = A (x + Jx) -> s, B (x - Jx) -> d */
+    static_assert(TM == 1 || (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0),
+                  "two threads per line need the split z phase");
     if constexpr (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0) {
-        z_split2<NX, NZ>(reinterpret_cast<float *>(X), reinterpret_cast<const float *>(KA),
+        z_split2<NX, NZ, TM>(reinterpret_cast<float *>(X), reinterpret_cast<const float *>(KA),
                          reinterpret_cast<const float *>(KB), tid);
     } else {
         P *row = X + tid * ZP;
@@ -602,13 +615,16 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         T2 bb[ITEMS * N1];
 #pragma unroll
         for (int it = 0; it < ITEMS; ++it) {
-            const int w = tid + it * NX, n2 = w / NZ2, c = w - n2 * NZ2;
+            const int w = tid + it * T, n2 = w / NZ2, c = w - n2 * NZ2;
+            if (ITEMS_EVEN || w < N2 * NZ2) {
 #pragma unroll
-            for (int n1 = 0; n1 < N1; ++n1) bb[it * N1 + n1] = b2p[(N2 * n1 + n2) * NZ2 + c];
+                for (int n1 = 0; n1 < N1; ++n1) bb[it * N1 + n1] = b2p[(N2 * n1 + n2) * NZ2 + c];
+            }
         }
 #pragma unroll
         for (int it = 0; it < ITEMS; ++it) {
-            const int w = tid + it * NX, n2 = w / NZ2, c = w - n2 * NZ2;
+            const int w = tid + it * T, n2 = w / NZ2, c = w - n2 * NZ2;
+            if (!ITEMS_EVEN && w >= N2 * NZ2) break;
             Cx<P> v[N1];
 #pragma unroll
             for (int n1 = 0; n1 < N1; ++n1) {
@@ -630,7 +646,8 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
             for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
         }
     } else {
-        constexpr int PER = NZ2; /* pairs per thread */
+        static_assert(NZ2 % TM == 0, "pairs must split evenly over the threads");
+        constexpr int PER = NZ2 / TM; /* pairs per thread */
         constexpr int BATCH = PER;
         const T2 *b2p = reinterpret_cast<const T2 *>(bz);
         const T2 *n2p = reinterpret_cast<const T2 *>(bnext);
@@ -638,10 +655,10 @@ __global__ void __launch_bounds__(NX) k_chain2d(Step2DArgs a)
         for (int j0 = 0; j0 < PER; j0 += BATCH) {
             T2 bb[BATCH];
 #pragma unroll
-            for (int j = 0; j < BATCH; ++j) bb[j] = b2p[tid + (j0 + j) * NX];
+            for (int j = 0; j < BATCH; ++j) bb[j] = b2p[tid + (j0 + j) * T];
 #pragma unroll
             for (int j = 0; j < BATCH; ++j) {
-                const int e = tid + (j0 + j) * NX;
+                const int e = tid + (j0 + j) * T;
                 const int x = e / NZ2, c = e - x * NZ2;
                 T2 &slot = reinterpret_cast<T2 *>(X)[x * ZP2 + c];
                 T2 o = slot;
@@ -666,14 +683,32 @@ static size_t smem_bytes_t()
     return Smem2D<P, NX, NZ>::END;
 }
 
+/* Two threads per line where the z phase is the split one (NZ/2 a multiple of 8). */
+template <int NX, int NZ>
+struct WideOk {
+    static constexpr bool value = (NZ / 2) % 8 == 0 && SCFT_F32X2;
+};
+
 template <typename P, int NX, int NZ, int N1, int N2>
-static cudaError_t launch_t(const Step2DArgs &a, int nblocks, cudaStream_t st, int configure)
+static cudaError_t launch_t(const Step2DArgs &a, int nblocks, cudaStream_t st, int configure, int wide)
 {
     const size_t smem = smem_bytes_t<P, NX, NZ, N1, N2>();
-    if (configure)
-        return cudaFuncSetAttribute(k_chain2d<P, NX, NZ, N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem);
-    k_chain2d<P, NX, NZ, N1, N2><<<nblocks, NX, smem, st>>>(a);
+    if (configure) {
+        cudaError_t e = cudaFuncSetAttribute(k_chain2d<P, NX, NZ, N1, N2, 1>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if constexpr (WideOk<NX, NZ>::value)
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_chain2d<P, NX, NZ, N1, N2, 2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return e;
+    }
+    if constexpr (WideOk<NX, NZ>::value) {
+        if (wide) {
+            k_chain2d<P, NX, NZ, N1, N2, 2><<<nblocks, 2 * NX, smem, st>>>(a);
+            return cudaGetLastError();
+        }
+    }
+    k_chain2d<P, NX, NZ, N1, N2, 1><<<nblocks, NX, smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -703,14 +738,28 @@ size_t scft_step2d_smem(int prec, int nx, int nz)
     return 0;
 }
 
-/* configure = 1 raises the kernel's shared-memory limit (call once, outside
- * any stream capture); configure = 0 launches. */
+/* 1 if the shape has the two-threads-per-line kernel (bit-identical results,
+ * for batches of at most one chain per SM). */
+int scft_step2d_wide(int prec, int nx, int nz)
+{
+    if (prec == SCFT_PREC_FP64) return 0;
+#define X(NX_, NZ_, A_, B_) \
+    if (nx == NX_ && nz == NZ_) return WideOk<NX_, NZ_>::value ? 1 : 0;
+    SCFT_STEP2D_SHAPES(X)
+#undef X
+    return 0;
+}
+
+/* configure = 1 raises the kernels' shared-memory limit (call once, outside
+ * any stream capture); configure = 0 launches, with two threads per line if
+ * wide is set and the shape has that kernel. */
 cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, int nblocks, cudaStream_t st,
-                               int configure)
+                               int configure, int wide)
 {
 #define X(NX_, NZ_, A_, B_)                                                                                           \
     if (nx == NX_ && nz == NZ_)                                                                                        \
-        return prec == SCFT_PREC_FP64 ? cudaErrorInvalidValue : launch_t<float, NX_, NZ_, A_, B_>(a, nblocks, st, configure);
+        return prec == SCFT_PREC_FP64 ? cudaErrorInvalidValue                                                         \
+                                      : launch_t<float, NX_, NZ_, A_, B_>(a, nblocks, st, configure, wide);
     SCFT_STEP2D_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;

@@ -251,7 +251,8 @@ class Solver:
         t = L.CTiming()
         L.check(L.lib().scft_get_timing(self._h, C.byref(t)), "scft_get_timing")
         return {"total_ms": t.total_ms, "prop_ms": t.prop_ms, "prop_launches": t.prop_launches,
-                "kernel_launches": t.kernel_launches, "fused_chain": int(t.fused_chain)}
+                "kernel_launches": t.kernel_launches, "fused_chain": int(t.fused_chain),
+                "threads_per_line": int(t.threads_per_line)}
 
 
 # ----------------------------------------------------------------- host side

@@ -58,3 +58,34 @@ def test_fused_iterations_film(srn, golden):
     by_iter = {rec.iter: rec for rec in r.records}
     for row in g["free_energy"]:
         assert abs(by_iter[int(row[0])].free_energy - row[1]) <= 1e-6 * max(1.0, abs(row[1]))
+
+
+@pytest.mark.parametrize("nx,nz", [(192, 96), (192, 128), (128, 96), (96, 64), (64, 32)])
+def test_two_threads_per_line_bit_identical(srn, nx, nz):
+    """A batch of at most one chain per SM gives every line two threads; an
+    instance must come out bit for bit as it does in a batch too large for
+    that (one thread per line): records, fields and densities."""
+    s = srn.configs.film2d(nx=nx, nz=nz, ns=40, iters=3)
+    w = srn.configs.droplet_fields(s, seed=7, radius=nx * 0.125 / 5)
+    m = srn.configs.substrate_mask(s)
+
+    def run(B):
+        with srn.Solver([s] * B, precision="fp32") as sv:
+            tpl = sv.timing()["threads_per_line"]
+            for b in range(B):
+                sv.set_fields(w, b)
+                sv.set_masks(m, b)
+                sv.set_iteration(1, b)
+            out = sv.iterate(3)
+            phi, tot = sv.get_densities(0)
+            return tpl, [r[0] for r in out], sv.get_fields(0), phi, tot
+
+    t1, o1, w1, p1, s1 = run(1)
+    tb, ob, wb, pb, sb = run(40)          # 40 instances x 5 chains: more chains than SMs
+    assert t1 == 2 and tb == 1
+    for a, b in zip(o1, ob):
+        assert a.free_energy == b.free_energy and a.rms == b.rms
+        np.testing.assert_array_equal(a.q, b.q)
+    np.testing.assert_array_equal(w1, wb)
+    np.testing.assert_array_equal(p1, pb)
+    np.testing.assert_array_equal(s1, sb)
