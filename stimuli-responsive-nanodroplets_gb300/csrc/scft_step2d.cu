@@ -1,11 +1,17 @@
 /*
- * scft_step2d.cu — one fused launch per contour step for 2D (NY = 1) grids:
+ * scft_step2d.cu — the whole contour loop of a chain in one persistent launch
+ * for 2D (NY = 1) grids, FP32:
  *   q_{s+1} = b . Kz . Kx . (b . q_s),   b = exp(-DS w / 2)
  * (funPDESolver_periodic / funPDESolver_DirichletBC, SCFT.c:2474-2631).
  *
  * One CTA owns one NX x NZ slice of one chain of one instance, entirely in
- * shared memory (row pitch NZ+2 keeps the 64/128-bit row accesses of the z
- * phase conflict-free), so a step reads q_s and b once and writes q_{s+1} once.
+ * shared memory for all of the chain's steps (row pitch NZ+2 keeps the
+ * 64/128-bit row accesses of the z phase conflict-free), so a step reads b
+ * once and writes q_{s+1} once; q_s never comes back from HBM. The store phase
+ * of a step also runs the next step's first FFT phase (below) on the values it
+ * has in registers. A CTA has one thread per line, or two (TM = 2) when the
+ * batch has at most one chain per SM: every value is then computed by the
+ * same arithmetic on another thread, so results do not depend on TM.
  *
  *  x axis (periodic): pairs of adjacent z columns form one complex column, as
  *  the factor is real and even in k. Each complex column of length N = NX =
