@@ -23,6 +23,40 @@ def test_library_exports_every_header_symbol(srn):
     assert not missing, missing
 
 
+def test_ctypes_layouts_match_header(tmp_path):
+    """Every public struct of include/scft_gpu.h has the size and field offsets
+    that the ctypes mirror in _lib.py assumes (a C program built against the
+    header prints them)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    L = importlib.import_module("stimuli-responsive-nanodroplets_gb300._lib")
+    structs = {"scft_surface": L.CSurface, "scft_derived": L.CDerived, "scft_options": L.COptions,
+               "scft_iter_out": L.CIterOut, "scft_batch_result": L.CBatchResult, "scft_timing": L.CTiming}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "scft_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            parts = line.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
 @pytest.mark.parametrize("case", CASES)
 def test_derive_matches_oracle(case, srn, golden, oracle_mod):
     g = golden(case)
