@@ -151,6 +151,26 @@ def case_blend3d():
     return s, w, None
 
 
+def case_blend3d_full():
+    """The four-diblock blend at its full size (64^3, NS 128, noise on) for its
+    first six iterations from the bench's start. Only the per-iteration series
+    are stored; the test regenerates the start fields from the same seed."""
+    s = srn.configs.blend3d(seed=2, iters=6)
+    s.D_WRT = 1000
+    w = srn.configs.uniform_fields(s.grid(), seed=1000, amp=0.1, fields=tuple(range(9)))
+    return s, w
+
+
+def collect_series(name, s, d: Path, w14, counter, seed):
+    fe = np.array([[float(x) for x in l.split()] for l in (d / "free_energy.dat").read_text().splitlines() if l.strip()])
+    en = np.array([[float(x) for x in l.split()] for l in (d / "energies.dat").read_text().splitlines() if l.strip()])
+    dv = np.array([[float(x) for x in l.split()] for l in (d / "deviations.dat").read_text().splitlines() if l.strip()])
+    np.savez_compressed(GOLD / f"{name}.npz", surface=json.dumps(s.__dict__), counter=counter, seed0=np.array(seed),
+                        w_sum=w14.sum(axis=1), w_sumsq=(w14 * w14).sum(axis=1), free_energy=fe, energies=en,
+                        deviations=dv)
+    print(f"{name}: {len(fe)} iterations (series only)")
+
+
 def case_quirks():
     """Even homopolymer contour count (LEN > 1), brush field active with MASK 0,
     energies every 2nd iteration."""
@@ -257,6 +277,12 @@ def kat_density(tag: str, s, ns: int, blocks, seed: int):
 def main():
     if not obuild.reference_available():
         raise SystemExit(f"reference source not found at {obuild.REFERENCE_SRC}")
+    if sys.argv[1:] == ["blend3d_full"]:
+        # the full-size blend alone (about six minutes of one core)
+        s, w = case_blend3d_full()
+        d, _ = run_case("blend3d_full", s, w)
+        collect_series("blend3d_full", s, d, w, 1, (11, 22, 33))
+        return
     for name, fn in (("bulk2d", case_bulk2d), ("film2d", case_film2d), ("blend3d", case_blend3d),
                      ("quirks", case_quirks)):
         s, w, mask3 = fn()

@@ -231,3 +231,28 @@ def test_density_unit_matches_funDensity(srn, precision):
         for (start, stop), phi in zip(g["blocks"], g["phi"]):
             got = sv.density(g["qf"], g["qb"], int(start), int(stop), float(g["Q"]))
             np.testing.assert_allclose(got, phi, rtol=tol, atol=0)
+
+
+def test_blend3d_full_size_matches_reference(srn):
+    """The four-diblock blend at its full size (64^3, NS 128, 11 chains, noise
+    from the drand48 replay) against the reference's own first six iterations
+    from the bench's start: free energy, chemical potentials and RMS."""
+    g = load_golden("blend3d_full")
+    S = surface_from_json(srn, g["surface"])
+    w0 = srn.configs.uniform_fields(S.grid(), seed=1000, amp=0.1, fields=tuple(range(9)))
+    # the start must be the reference's: the generator's stream is checked, not trusted
+    np.testing.assert_allclose(w0.sum(axis=1), g["w_sum"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose((w0 * w0).sum(axis=1), g["w_sumsq"], rtol=1e-14, atol=0)
+    r = runner_mod().Run(S, w0, int(g["counter"]), tuple(int(x) for x in g["seed0"]), None, precision="fp64",
+                         noise="device")
+    r.run_to_end()
+    by_iter = {rec.iter: rec for rec in r.records}
+    assert len(g["free_energy"]) == 6
+    for row in g["free_energy"]:
+        rec = by_iter[int(row[0])]
+        assert abs(rec.free_energy - row[1]) <= F_RTOL * abs(row[1]), (row[0], rec.free_energy, row[1])
+    for row in g["energies"]:
+        np.testing.assert_allclose(by_iter[int(row[0])].mu, row[1:], rtol=1e-10, atol=1e-11)
+    for row in g["deviations"]:
+        rec = by_iter[int(row[0])]
+        assert abs(rec.rms - row[1]) <= 1e-8 * abs(row[1]), (row[0], rec.rms, row[1])
