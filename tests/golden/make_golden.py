@@ -161,6 +161,27 @@ def case_blend3d_full():
     return s, w
 
 
+def case_film2d_full():
+    """The thin-film droplet configuration at its full size (192x1x96, NS 128,
+    MASK 1) for six iterations from a seeded half-disk droplet start."""
+    s = srn.configs.film2d(iters=6)
+    s.D_WRT = 1000
+    w = srn.configs.droplet_fields(s, seed=1000)
+    return s, w
+
+
+def case_bulk2d_full():
+    """The 2D bulk melt configuration at its full size (64x1x64, NS 100) for ten
+    iterations from a uniform[-0.1, 0.1] start on w_A, w_B."""
+    s = srn.configs.bulk2d(iters=10)
+    s.D_WRT = 1000
+    w = srn.configs.uniform_fields(s.grid(), seed=1000, amp=0.1, fields=(0, 1))
+    return s, w
+
+
+FULL_SERIES = {"blend3d_full": case_blend3d_full, "film2d_full": case_film2d_full, "bulk2d_full": case_bulk2d_full}
+
+
 def collect_series(name, s, d: Path, w14, counter, seed):
     fe = np.array([[float(x) for x in l.split()] for l in (d / "free_energy.dat").read_text().splitlines() if l.strip()])
     en = np.array([[float(x) for x in l.split()] for l in (d / "energies.dat").read_text().splitlines() if l.strip()])
@@ -277,11 +298,13 @@ def kat_density(tag: str, s, ns: int, blocks, seed: int):
 def main():
     if not obuild.reference_available():
         raise SystemExit(f"reference source not found at {obuild.REFERENCE_SRC}")
-    if sys.argv[1:] == ["blend3d_full"]:
-        # the full-size blend alone (about six minutes of one core)
-        s, w = case_blend3d_full()
-        d, _ = run_case("blend3d_full", s, w)
-        collect_series("blend3d_full", s, d, w, 1, (11, 22, 33))
+    if sys.argv[1:] and all(a in FULL_SERIES for a in sys.argv[1:]):
+        # full-size series alone (the blend takes about six minutes of one core)
+        for name in sys.argv[1:]:
+            s, w = FULL_SERIES[name]()
+            d, mask3 = run_case(name, s, w)
+            collect_series(name, s, d, w, 1, (11, 22, 33))
+            shutil.rmtree(d)  # the run folder holds full-size text files
         return
     for name, fn in (("bulk2d", case_bulk2d), ("film2d", case_film2d), ("blend3d", case_blend3d),
                      ("quirks", case_quirks)):

@@ -233,21 +233,33 @@ def test_density_unit_matches_funDensity(srn, precision):
             np.testing.assert_allclose(got, phi, rtol=tol, atol=0)
 
 
-def test_blend3d_full_size_matches_reference(srn):
-    """The four-diblock blend at its full size (64^3, NS 128, 11 chains, noise
-    from the drand48 replay) against the reference's own first six iterations
-    from the bench's start: free energy, chemical potentials and RMS."""
-    g = load_golden("blend3d_full")
+def _full_start(srn, name, S):
+    """The start fields and grafting mask each full-size series was generated from."""
+    if name == "blend3d_full":
+        return srn.configs.uniform_fields(S.grid(), seed=1000, amp=0.1, fields=tuple(range(9))), None
+    if name == "film2d_full":
+        return srn.configs.droplet_fields(S, seed=1000), srn.configs.substrate_mask(S)
+    return srn.configs.uniform_fields(S.grid(), seed=1000, amp=0.1, fields=(0, 1)), None
+
+
+@pytest.mark.parametrize("name", ["bulk2d_full", "film2d_full", "blend3d_full"])
+def test_full_size_configurations_match_reference(srn, name):
+    """Each configuration at its full size against the reference's own first
+    iterations from a seeded start: the 2D bulk melt (64x1x64, NS 100), the
+    thin-film droplet (192x1x96, NS 128, MASK 1, brush) and the four-diblock
+    blend (64^3, NS 128, 11 chains, noise from the drand48 replay): free energy,
+    chemical potentials and RMS of every iteration."""
+    g = load_golden(name)
     S = surface_from_json(srn, g["surface"])
-    w0 = srn.configs.uniform_fields(S.grid(), seed=1000, amp=0.1, fields=tuple(range(9)))
+    w0, mask3 = _full_start(srn, name, S)
     # the start must be the reference's: the generator's stream is checked, not trusted
     np.testing.assert_allclose(w0.sum(axis=1), g["w_sum"], rtol=0, atol=1e-9)
     np.testing.assert_allclose((w0 * w0).sum(axis=1), g["w_sumsq"], rtol=1e-14, atol=0)
-    r = runner_mod().Run(S, w0, int(g["counter"]), tuple(int(x) for x in g["seed0"]), None, precision="fp64",
+    r = runner_mod().Run(S, w0, int(g["counter"]), tuple(int(x) for x in g["seed0"]), mask3, precision="fp64",
                          noise="device")
     r.run_to_end()
     by_iter = {rec.iter: rec for rec in r.records}
-    assert len(g["free_energy"]) == 6
+    assert len(g["free_energy"]) >= 6
     for row in g["free_energy"]:
         rec = by_iter[int(row[0])]
         assert abs(rec.free_energy - row[1]) <= F_RTOL * abs(row[1]), (row[0], rec.free_energy, row[1])
