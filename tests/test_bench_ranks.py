@@ -47,3 +47,22 @@ def test_reference_arm_is_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(bench, "cpu_sample", lambda *a, **k: called.append(1) or (1.0, 1.0))
     bench.run_reference(Args, rank=1, world=2)
     assert not called and capsys.readouterr().out == ""
+
+
+def test_reference_arm_line(tmp_path):
+    """bench.py --impl reference times the CPU restatement of SCFT.c and prints
+    the contract's line: the same metric and unit, a cpu_baseline describing
+    the run, and an e2e with no host-device bytes."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "bulk2d",
+                          "--batch", "2", "--steps", "1", "--warmup", "0", "--cpu-threads", "2"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=300, check=True).stdout
+    line = json.loads(out.strip().splitlines()[-1])
+    import bench
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC
+    assert line["value"] > 0 and line["unit"] == "instance-iterations/s" and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
+    assert line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
