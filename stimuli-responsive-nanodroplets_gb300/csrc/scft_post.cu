@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
  * register-array indices are loop counters of fully unrolled loops.
  * Block partials of H, p and (phi_tot-1)^2 go to a.partial. */
 template <int NA>
-__global__ void __launch_bounds__(POST_THREADS, (NA <= 5 ? 2 : 1)) k_update(PostArgs a)
+__global__ void __launch_bounds__(POST_THREADS, (NA <= 4 ? 3 : 2)) k_update(PostArgs a)
 {
     __shared__ double sh[3 * 32];
     __shared__ double coef[SCFT_MAX_BLOCKS];
