@@ -329,7 +329,10 @@ __global__ void __launch_bounds__(POST_THREADS) k_density(PostArgs a)
  * the reference) and is not updated. The list, the chi sub-table and the block
  * factors sit in shared memory; per-point values stay in registers because all
  * register-array indices are loop counters of fully unrolled loops.
- * Block partials of H, p and (phi_tot-1)^2 go to a.partial. */
+ * Block partials of H, p and (phi_tot-1)^2 go to a.partial. The pass is bound
+ * by the FP64 pipe's latency, so it is built for three CTAs per SM with up to
+ * four active fields and two otherwise (a few registers spill; measured faster
+ * than one or two CTAs without spills). */
 template <int NA>
 __global__ void __launch_bounds__(POST_THREADS, (NA <= 4 ? 3 : 2)) k_update(PostArgs a)
 {
