@@ -294,12 +294,151 @@ static int pick_tile(long lines_per_chain, long inner_or_lines, int total_chains
     return tile;
 }
 
+/* bf16 round to nearest (ties to even) through FP32, and back */
+static uint16_t bf16_rn(long double v)
+{
+    const float f = (float)v;
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static long double bf16_val(uint16_t b)
+{
+    const uint32_t u = (uint32_t)b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return (long double)f;
+}
+
+/* Table of the tensor-core z operator of the fused FP32 2D loop (see
+ * scft_step2d.cu): y = Kb x + Kt x with Kb the band |j - k| <= 3 of K (circular
+ * for a periodic axis) and Kt = K - Kb.
+ *   bytes [0, 32 nz): float band[nz][8], slot d + 3 of row j multiplying
+ *     x[(j + d) mod nz], zero where a Dirichlet row has no such neighbour;
+ *   then the tail's centrosymmetric halves Ae = (Kt[i][k] + Kt[i][nz-1-k]) / 2,
+ *     Ao = (Kt[i][k] - Kt[i][nz-1-k]) / 2 (i, k < h), each split into bf16
+ *     pieces hi = rn(A), lo = rn(A - hi), stored Ae.hi, Ae.lo, Ao.hi, Ao.lo as
+ *     K-major 8 x 16-byte core matrices (element (i, k) at byte
+ *     (i/8) 16h + (k/8) 128 + (i%8) 16 + (k%8) 2).
+ * The band is rounded to FP32 so that every column sum of the operator the
+ * kernel applies (FP32 band plus the bf16 pieces' sums) equals the column sum
+ * of K as closely as FP32 allows, largest band entries moved first by one ulp
+ * at most (the reasoning of round_fp32_colsum: no systematic per-step gain of
+ * the dominant mode). */
+static std::vector<unsigned char> ztc_table(const std::vector<long double> &K, int nz, int periodic)
+{
+    const int h = nz / 2;
+    auto inband = [&](int j, int k) {
+        int d = j > k ? j - k : k - j;
+        if (periodic && nz - d < d) d = nz - d;
+        return d <= 3;
+    };
+    std::vector<long double> T(K);
+    for (int j = 0; j < nz; ++j)
+        for (int k = 0; k < nz; ++k)
+            if (inband(j, k)) T[(size_t)j * nz + k] = 0.0L;
+    std::vector<uint16_t> pc((size_t)4 * h * h);
+    std::vector<long double> Aeff((size_t)h * h), Oeff((size_t)h * h);
+    for (int i = 0; i < h; ++i)
+        for (int k = 0; k < h; ++k) {
+            const long double a = T[(size_t)i * nz + k], m = T[(size_t)i * nz + (nz - 1 - k)];
+            const long double ae = (a + m) / 2.0L, ao = (a - m) / 2.0L;
+            const uint16_t e1 = bf16_rn(ae), e2 = bf16_rn(ae - bf16_val(e1));
+            const uint16_t o1 = bf16_rn(ao), o2 = bf16_rn(ao - bf16_val(o1));
+            const size_t at = (size_t)i * h + k;
+            pc[0 * (size_t)h * h + at] = e1;
+            pc[1 * (size_t)h * h + at] = e2;
+            pc[2 * (size_t)h * h + at] = o1;
+            pc[3 * (size_t)h * h + at] = o2;
+            Aeff[at] = bf16_val(e1) + bf16_val(e2);
+            Oeff[at] = bf16_val(o1) + bf16_val(o2);
+        }
+    /* the tail the kernel applies, in full form, and the FP32 band */
+    std::vector<long double> Teff((size_t)nz * nz, 0.0L);
+    for (int i = 0; i < h; ++i)
+        for (int k = 0; k < h; ++k) {
+            const long double ae = Aeff[(size_t)i * h + k], ao = Oeff[(size_t)i * h + k];
+            Teff[(size_t)i * nz + k] = ae + ao;
+            Teff[(size_t)i * nz + (nz - 1 - k)] = ae - ao;
+            Teff[(size_t)(nz - 1 - i) * nz + k] = ae - ao;
+            Teff[(size_t)(nz - 1 - i) * nz + (nz - 1 - k)] = ae + ao;
+        }
+    std::vector<float> B((size_t)nz * nz, 0.0f);
+    std::vector<int> rows;
+    for (int k = 0; k < nz; ++k) {
+        long double target = 0.0L, have = 0.0L;
+        rows.clear();
+        for (int j = 0; j < nz; ++j) {
+            target += K[(size_t)j * nz + k];
+            have += Teff[(size_t)j * nz + k];
+            if (inband(j, k)) {
+                const float r = (float)K[(size_t)j * nz + k];
+                B[(size_t)j * nz + k] = r;
+                have += (long double)r;
+                rows.push_back(j);
+            }
+        }
+        std::sort(rows.begin(), rows.end(), [&](int x, int y) {
+            return fabsl(K[(size_t)x * nz + k]) > fabsl(K[(size_t)y * nz + k]);
+        });
+        long double resid = target - have;
+        for (int j : rows) {
+            if (resid == 0.0L) break;
+            const float r = B[(size_t)j * nz + k];
+            if (r == 0.0f) continue;
+            const float up = nextafterf(r, INFINITY), dn = nextafterf(r, -INFINITY);
+            const long double ulp_up = (long double)up - r, ulp_dn = (long double)r - dn;
+            if (resid >= ulp_up / 2) {
+                B[(size_t)j * nz + k] = up;
+                resid -= ulp_up;
+            } else if (-resid >= ulp_dn / 2) {
+                B[(size_t)j * nz + k] = dn;
+                resid += ulp_dn;
+            }
+        }
+    }
+    const size_t nb = (size_t)32 * nz, piece = (size_t)2 * h * h;
+    std::vector<unsigned char> out(nb + 4 * piece, 0);
+    float *band = reinterpret_cast<float *>(out.data());
+    for (int j = 0; j < nz; ++j)
+        for (int d = -3; d <= 3; ++d) {
+            int k = j + d;
+            if (k < 0 || k >= nz) {
+                if (!periodic) continue;
+                k = (k + nz) % nz;
+            }
+            band[(size_t)j * 8 + (d + 3)] = B[(size_t)j * nz + k];
+        }
+    for (int p = 0; p < 4; ++p)
+        for (int i = 0; i < h; ++i)
+            for (int k = 0; k < h; ++k) {
+                const size_t off = nb + p * piece + (size_t)(i / 8) * 16 * h + (size_t)(k / 8) * 128 + (i % 8) * 16 + (k % 8) * 2;
+                memcpy(out.data() + off, &pc[(size_t)p * h * h + (size_t)i * h + k], 2);
+            }
+    return out;
+}
+
 /* z operator halves and x factor of one operator set for the fused 2D step. */
 static int fused2d_tables(scft_ctx *c, const scft_derived &d, InstOps &o)
 {
     const int nz = d.nz, h = nz / 2, nx = d.nx;
     std::vector<long double> K;
     dense_operator(nz, d.alphaz, c->surf[0].mask, K);
+    if (scft_step2d_ztc(c->opt.precision, nx, nz)) {
+        std::vector<double> ex(nx);
+        for (int k = 0; k < nx; ++k) {
+            const double kk = kval(k, nx);
+            ex[k] = exp(-d.alphax * kk * kk) / nx;
+        }
+        void *kz_d = nullptr, *ex_d = nullptr;
+        int rc = upload(c, &kz_d, ztc_table(K, nz, !c->surf[0].mask));
+        if (!rc) rc = upload_p(c, &ex_d, ex);
+        if (rc) return rc;
+        o.kz = kz_d;
+        o.ex = ex_d;
+        return SCFT_OK;
+    }
     std::vector<double> kz((size_t)2 * h * h);
     for (int i = 0; i < h; ++i)
         for (int j = 0; j < h; ++j) {
@@ -1337,7 +1476,10 @@ static int collect_chunk(scft_ctx *c, scft_iter_out *out)
     if (chunk > 0)
         for (int b = 0; b < c->B; ++b) c->iter[b] = c->hist_host[(size_t)(chunk - 1) * c->B + b].iter;
     if (status != SCFT_OK) {
-        set_err("non-finite Q, free energy or RMS");
+        if (c->fused2d && scft_step2d_take_fault())
+            set_err("non-finite Q, free energy or RMS (a tensor-core wait of the contour loop gave up)");
+        else
+            set_err("non-finite Q, free energy or RMS");
         return status;
     }
     return SCFT_OK;

@@ -178,8 +178,10 @@ struct Step2DArgs {
     int s_end;         /* runs steps s .. min(s_end, len-1)-1 */
     long sstride;      /* slice stride (elements) */
     /* per chain through ChainDesc::ops: kz P[2*H*H] (A[i][k] then B[i][k],
-     * H = NZ/2), twx Cx<P>[NX] (exp(-2 pi i n2 k1 / NX) at n2*N1 + k1), ex
-     * P[NX] (E_x(k)/NX) */
+     * H = NZ/2) or, where scft_step2d_ztc is 1, float band[NZ][8] followed by
+     * the bf16 pieces Ae1, Ae2, Ao1, Ao2 of the tail (H x H each, K-major
+     * core-matrix layout); twx Cx<P>[NX] (exp(-2 pi i n2 k1 / NX) at
+     * n2*N1 + k1), ex P[NX] (E_x(k)/NX) */
 };
 
 size_t scft_step2d_smem(int prec, int nx, int nz);
@@ -191,6 +193,10 @@ cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, in
                                int configure, int wide);
 /* 1 if (nx, nz) has the two-threads-per-line form of the fused 2D loop */
 int scft_step2d_wide(int prec, int nx, int nz);
+/* 1 if the fused 2D loop of (nx, nz) runs the z tail on the tensor cores */
+int scft_step2d_ztc(int prec, int nx, int nz);
+/* 1 if a tensor-core wait of the 2D loop gave up since the last call (clears it) */
+int scft_step2d_take_fault(void);
 
 /* Internal hooks of scft_ctx.cu for the allocation-free propagator entry point. */
 int scft_ctx_info(const scft_ctx *c, int *device, int *prec, long *m, long *sm, double *ds, cudaStream_t *st,

@@ -75,16 +75,46 @@ struct Cx {
 
 constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
 
-/* byte offsets of the shared-memory regions: X, KA, KB, TW, EX */
+/* The z operator runs on the tensor cores (band on the FP32 pipe, tail by
+ * tcgen05.mma) for FP32 shapes whose half size is a multiple of 16 (the MMA's
+ * K step and N granule) and whose lines fill at most two 128-row tiles. */
+template <typename P, int NX, int NZ>
+struct ZTcOk {
+    static constexpr bool value = sizeof(P) == 4 && (NZ / 2) % 16 == 0 && NX % 32 == 0 && NX <= 256;
+};
+
+/* TMEM columns of the tensor-core z tail: D = [Pe | Po] (H columns each,
+ * FP32), then the A operand pieces U1, U2, V1, V2 (bf16 pairs, H/2 columns
+ * each). */
+template <int NZ>
+struct ZTail {
+    static constexpr int H = NZ / 2;
+    static constexpr int PC = H / 2;
+    static constexpr int COL_PE = 0, COL_PO = H, COL_A = 2 * H;
+    static constexpr int USED = 2 * H + 4 * PC;
+    static constexpr int TCOLS = USED <= 32 ? 32 : USED <= 64 ? 64 : USED <= 128 ? 128 : USED <= 256 ? 256 : 512;
+    static constexpr int PIECE = 2 * H * H;      /* bytes of one H x H bf16 operator piece */
+    static constexpr int SBO = 16 * H;           /* bytes between 8-row core-matrix groups */
+    static constexpr int LBO = 128;              /* bytes between K-adjacent core matrices */
+    static constexpr int BAND = 8;               /* band coefficients per output row (7 used) */
+};
+
+/* byte offsets of the shared-memory regions: X, KA, KB, TW, EX; with the
+ * tensor-core z tail KA..KB holds the four bf16 operator pieces (the same 8 H^2
+ * bytes), followed by the band coefficients, the mbarrier and the TMEM slot */
 template <typename P, int NX, int NZ>
 struct Smem2D {
+    static constexpr bool TC = ZTcOk<P, NX, NZ>::value;
     static constexpr size_t H = NZ / 2;
     static constexpr size_t X = 0;
     static constexpr size_t KA = align16(X + sizeof(P) * NX * (NZ + 2));
     static constexpr size_t KB = align16(KA + sizeof(P) * H * H);
     static constexpr size_t TW = align16(KB + sizeof(P) * H * H);
     static constexpr size_t EX = align16(TW + 2 * sizeof(P) * NX);
-    static constexpr size_t END = align16(EX + sizeof(P) * NX);
+    static constexpr size_t BAND = align16(EX + sizeof(P) * NX);
+    static constexpr size_t MBAR = TC ? align16(BAND + sizeof(float) * NZ * ZTail<NZ>::BAND) : BAND;
+    static constexpr size_t END = TC ? align16(MBAR + 16) : BAND;
+    static_assert(!TC || 8 * H * H == KB - KA + sizeof(P) * H * H, "the bf16 pieces fill KA and KB");
 };
 
 template <typename P>
@@ -363,7 +393,220 @@ __device__ __forceinline__ void z_split2(float *X, const float *KA, const float 
     }
 }
 
+/* ------------------------------------------ z operator on the tensor cores
+ * y = Kb x + Kt x. Kb is the band |j - k| <= 3 of the operator (circular for a
+ * periodic axis), applied in FP32 with round-to-nearest FMAs; it carries all
+ * but ~0.3 % of every row's weight. Kt = K - Kb, the tail, is applied as its
+ * centrosymmetric halves (Pe = U Ae^T, Po = V Ao^T with u = x + Jx, v = x - Jx)
+ * by tcgen05.mma on bf16 pairs: u = u1 + u2 and Ae = Ae1 + Ae2 (16 bits each),
+ * three products per half (u2 Ae1 + u1 Ae2 + u1 Ae1), FP32 accumulation in
+ * TMEM. The tensor cores' accumulation truncates, but only on the tail, so its
+ * bias is ~3e-3 of an FP32 ulp of y per step; the split's own error is ~2^-17
+ * of the tail, below FP32 rounding of y. Lines are the MMA's M rows: lines
+ * 0..127 form tile 0 (TMEM lanes = line), lines 128..255 tile 1 (lanes =
+ * line - 128), run one after the other through the same TMEM columns. */
+__device__ __forceinline__ uint32_t bf16x2_rn(float hi, float lo)
+{
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+__device__ __forceinline__ float bf16_lo(uint32_t p) { return __uint_as_float(p << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t p) { return __uint_as_float(p & 0xffff0000u); }
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tm_st8(uint32_t ta, const uint32_t (&r)[8])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tm_ld16(uint32_t ta, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(ta)
+                 : "memory");
+}
+
+/* shared-memory matrix descriptor: K-major, no swizzle, 8 x 16-byte core matrices */
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+                 "r"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+/* Bounded wait for the mbarrier phase of the given parity: false after ~0.1 s. */
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, P1;\n\t}"
+                     : "=r"(done)
+                     : "r"(mb), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (clock64() - t0 > (1LL << 28)) return false;
+    }
+}
+
+/* u, v of one line split into bf16 pairs and stored to the A columns of its
+ * TMEM lane (ta = lane address of column COL_A); the line is read from shared
+ * memory 16 columns (and their mirror images) at a time. */
+template <int NZ>
+__device__ __forceinline__ void ztc_store_a(const float *row, uint32_t ta)
+{
+    using Z = ZTail<NZ>;
+#pragma unroll
+    for (int c = 0; c < Z::H / 16; ++c) {
+        float lo[16], hi[16]; /* x[16c + i], x[NZ - 16 - 16c + i] */
+#pragma unroll
+        for (int i = 0; i < 16; i += 2) {
+            const float2 a = *reinterpret_cast<const float2 *>(row + 16 * c + i);
+            const float2 m = *reinterpret_cast<const float2 *>(row + NZ - 16 - 16 * c + i);
+            lo[i] = a.x;
+            lo[i + 1] = a.y;
+            hi[i] = m.x;
+            hi[i + 1] = m.y;
+        }
+        uint32_t u1[8], u2[8], v1[8], v2[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            /* k = 16c + 2j: x[k], x[k+1] and their mirrors x[NZ-1-k], x[NZ-2-k] */
+            const float xa = lo[2 * j], xb = lo[2 * j + 1], ma = hi[15 - 2 * j], mb = hi[14 - 2 * j];
+            const float ua = xa + ma, ub = xb + mb, va = xa - ma, vb = xb - mb;
+            u1[j] = bf16x2_rn(ub, ua); /* even k in the low half */
+            v1[j] = bf16x2_rn(vb, va);
+            u2[j] = bf16x2_rn(ub - bf16_hi(u1[j]), ua - bf16_lo(u1[j]));
+            v2[j] = bf16x2_rn(vb - bf16_hi(v1[j]), va - bf16_lo(v1[j]));
+        }
+        tm_st8(ta + 0 * Z::PC + 8 * c, u1);
+        tm_st8(ta + 1 * Z::PC + 8 * c, u2);
+        tm_st8(ta + 2 * Z::PC + 8 * c, v1);
+        tm_st8(ta + 3 * Z::PC + 8 * c, v2);
+    }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+/* One thread issues the tail products of one tile and commits them to mb. */
+template <int NZ>
+__device__ __forceinline__ void ztc_issue(uint32_t tmem, uint32_t pieces, uint32_t mb)
+{
+    using Z = ZTail<NZ>;
+    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(Z::H >> 3) << 17) | (8u << 24);
+#pragma unroll
+    for (int c = 0; c < Z::H / 16; ++c) {
+        const uint32_t acc0 = c > 0;
+        const uint32_t aU1 = tmem + Z::COL_A + 8 * c, aU2 = aU1 + Z::PC, aV1 = aU1 + 2 * Z::PC, aV2 = aU1 + 3 * Z::PC;
+        const uint32_t off = 256u * c;
+        const uint64_t e1 = smem_desc(pieces + 0 * Z::PIECE + off, Z::LBO, Z::SBO);
+        const uint64_t e2 = smem_desc(pieces + 1 * Z::PIECE + off, Z::LBO, Z::SBO);
+        const uint64_t o1 = smem_desc(pieces + 2 * Z::PIECE + off, Z::LBO, Z::SBO);
+        const uint64_t o2 = smem_desc(pieces + 3 * Z::PIECE + off, Z::LBO, Z::SBO);
+        mma_bf16(tmem + Z::COL_PE, aU2, e1, IDESC, acc0);
+        mma_bf16(tmem + Z::COL_PE, aU1, e2, IDESC, 1u);
+        mma_bf16(tmem + Z::COL_PE, aU1, e1, IDESC, 1u);
+        mma_bf16(tmem + Z::COL_PO, aV2, o1, IDESC, acc0);
+        mma_bf16(tmem + Z::COL_PO, aV1, o2, IDESC, 1u);
+        mma_bf16(tmem + Z::COL_PO, aV1, o1, IDESC, 1u);
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+}
+
+/* Band part of one line, written over the line in place: coefficient slot
+ * d + 3 of row j multiplies x[(j + d) mod NZ] (zero where a Dirichlet row has
+ * no such neighbour); small terms first. A window x[j-3 .. j+5] moves along
+ * the line in registers, so every value is read before its slot is written;
+ * the last two pairs wrap to the saved head of the line. */
+template <int NZ>
+__device__ __forceinline__ void ztc_band(float *row, const float *bt)
+{
+    const float4 *b4 = reinterpret_cast<const float4 *>(bt);
+    const float2 h01 = *reinterpret_cast<const float2 *>(row);
+    const float2 h23 = *reinterpret_cast<const float2 *>(row + 2);
+    const float2 t0 = *reinterpret_cast<const float2 *>(row + NZ - 4);
+    const float2 t1 = *reinterpret_cast<const float2 *>(row + NZ - 2);
+    const float head[4] = {h01.x, h01.y, h23.x, h23.y};
+    float w[9]; /* w[i] = x[j - 3 + i] */
+    w[0] = t0.y;
+    w[1] = t1.x;
+    w[2] = t1.y;
+    w[3] = head[0];
+    w[4] = head[1];
+    w[5] = head[2];
+    w[6] = head[3];
+    auto pair = [&](int j) {
+        float y[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float4 ca = b4[2 * (j + e)], cb = b4[2 * (j + e) + 1];
+            const float *x = w + e; /* x[d + 3] = x_{j+e+d} */
+            float t = ca.x * x[0];
+            t = fmaf(cb.z, x[6], t);
+            t = fmaf(ca.y, x[1], t);
+            t = fmaf(cb.y, x[5], t);
+            t = fmaf(ca.z, x[2], t);
+            t = fmaf(cb.x, x[4], t);
+            y[e] = fmaf(ca.w, x[3], t);
+        }
+        *reinterpret_cast<float2 *>(row + j) = make_float2(y[0], y[1]);
+#pragma unroll
+        for (int i = 0; i < 7; ++i) w[i] = w[i + 2];
+    };
+#pragma unroll 4
+    for (int j = 0; j < NZ - 4; j += 2) {
+        const float2 n = *reinterpret_cast<const float2 *>(row + j + 4);
+        w[7] = n.x;
+        w[8] = n.y;
+        pair(j);
+    }
+    w[7] = head[0];
+    w[8] = head[1];
+    pair(NZ - 4);
+    w[7] = head[2];
+    w[8] = head[3];
+    pair(NZ - 2);
+}
+
+/* Adds the tail (Pe + Po on top, Pe - Po mirrored below) to the band values of
+ * the line (td = lane address of column 0). */
+template <int NZ>
+__device__ __forceinline__ void ztc_combine(float *row, uint32_t td)
+{
+    using Z = ZTail<NZ>;
+#pragma unroll
+    for (int c0 = 0; c0 < Z::H; c0 += 16) {
+        uint32_t pe[16], po[16];
+        tm_ld16(td + Z::COL_PE + c0, pe);
+        tm_ld16(td + Z::COL_PO + c0, po);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const float e = __uint_as_float(pe[i]), o = __uint_as_float(po[i]);
+            row[c0 + i] += e + o;
+            row[NZ - 1 - c0 - i] += e - o;
+        }
+    }
+}
+
 } // namespace
+
+/* Set when a tensor-core wait of the chain kernel gave up (the chain's slice
+ * is then written as NaN, so the instance reports a non-finite status). */
+__device__ int g_scft_tc_fault;
 
 /* ------------------------------------------------------------------ kernel */
 /* 16-byte asynchronous copy global -> shared (no register staging) */
@@ -377,8 +620,20 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
  * the slice stays in shared memory from step to step (q_{s+1} is written to
  * HBM for the densities and kept for the next step), the operator tables are
  * loaded once. Chains are taken longest first through a.order. */
+/* CTAs per SM the loop is compiled for (one thread per line): as many as the
+ * shared memory and, with the tensor-core z tail, the TMEM columns allow, at
+ * most 4; the register budget per thread follows from it. */
+template <typename P, int NX, int NZ, int TM>
+struct MinBlocks2D {
+    static constexpr long S = (long)Smem2D<P, NX, NZ>::END + 1024;
+    static constexpr long by_smem = 233472 / S;
+    static constexpr long by_tmem = Smem2D<P, NX, NZ>::TC ? 512 / ZTail<NZ>::TCOLS : 8;
+    static constexpr long v = by_smem < by_tmem ? by_smem : by_tmem;
+    static constexpr int value = TM > 1 ? 1 : (v < 1 ? 1 : (v > 4 ? 4 : (int)v));
+};
+
 template <typename P, int NX, int NZ, int N1, int N2, int TM>
-__global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
+__global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) k_chain2d(Step2DArgs a)
 {
     constexpr int T = NX * TM; /* threads: TM per line */
     static_assert(N1 * N2 == NX, "NX = N1 * N2");
@@ -410,13 +665,22 @@ __global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
     constexpr int ITEMS = (N2 * NZ2 + T - 1) / T;
     constexpr bool ITEMS_EVEN = (N2 * NZ2) % T == 0;
 
+    constexpr bool ZTC = L::TC;
     /* operators and tables, once per chain (16-byte asynchronous copies) */
     {
         constexpr int VP = 16 / sizeof(P);
         const P *gA = reinterpret_cast<const P *>(cd.ops->kz);
-        for (int e = tid; e < H * H / VP; e += T) {
-            cp_async16(KA + e * VP, gA + e * VP);
-            cp_async16(KB + e * VP, gA + H * H + e * VP);
+        if constexpr (ZTC) {
+            /* band coefficients [NZ][8] FP32, then the four bf16 pieces (8 H^2 bytes) */
+            constexpr int NB = NZ * ZTail<NZ>::BAND / 4, NP = 8 * H * H / 16;
+            const unsigned char *g = reinterpret_cast<const unsigned char *>(gA);
+            for (int e = tid; e < NB; e += T) cp_async16(smem_raw + L::BAND + 16 * e, g + 16 * e);
+            for (int e = tid; e < NP; e += T) cp_async16(smem_raw + L::KA + 16 * e, g + 16 * NB + 16 * e);
+        } else {
+            for (int e = tid; e < H * H / VP; e += T) {
+                cp_async16(KA + e * VP, gA + e * VP);
+                cp_async16(KB + e * VP, gA + H * H + e * VP);
+            }
         }
         const P *gT = reinterpret_cast<const P *>(cd.ops->twx);
         for (int e = tid; e < 2 * NX / VP; e += T) cp_async16(reinterpret_cast<P *>(TW) + e * VP, gT + e * VP);
@@ -434,8 +698,33 @@ __global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(reinterpret_cast<const T2 *>(qs) + e));
     }
     asm volatile("cp.async.commit_group;\n" ::);
+    /* tensor-core z tail: the mbarrier, the TMEM base address and the fault
+     * flag of this CTA live in shared memory (no registers across the loop) */
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem_raw + L::MBAR + 8);
+    int *fault_flag = reinterpret_cast<int *>(smem_raw + L::MBAR + 12);
+    if constexpr (ZTC) {
+        const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(smem_raw + L::MBAR);
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            *fault_flag = 0;
+        }
+        if (tid < 32) {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                             (uint32_t)__cvta_generic_to_shared(tslot)),
+                         "r"(ZTail<NZ>::TCOLS)
+                         : "memory");
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        }
+    }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    if constexpr (ZTC) {
+        /* the operator pieces are read by the tensor cores (async proxy) */
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+    }
     __syncthreads();
+    if constexpr (ZTC) tc_fence_after();
 
     /* the first step's input b . q_s; later steps get theirs from the store phase */
     {
@@ -513,7 +802,57 @@ __global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
     /* z: one row per thread, y = A (x + Jx) -> s, B (x - Jx) -> d */
     static_assert(TM == 1 || (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0),
                   "two threads per line need the split z phase");
-    if constexpr (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0) {
+    if constexpr (ZTC) {
+        /* band on the FP32 pipe, tail on the tensor cores; lines are the
+         * threads tid < NX (with TM = 2 the second group waits at the barriers) */
+        constexpr int NTILE = (NX + 127) / 128;
+        const bool line_thr = tid < NX;
+        const int tile = tid >> 7;
+        const uint32_t lane = (uint32_t)(tid & 96) << 16; /* 32 * (warp % 4): this warp's TMEM lanes */
+        const uint32_t pieces = (uint32_t)__cvta_generic_to_shared(smem_raw + L::KA);
+        const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(smem_raw + L::MBAR);
+        const uint32_t tmem = *tslot;
+        uint32_t ncommit = (uint32_t)(s - a.s) * NTILE; /* tail commits before this step */
+        float *row = reinterpret_cast<float *>(X) + (line_thr ? tid : 0) * ZP;
+        const float *bt = reinterpret_cast<const float *>(smem_raw + L::BAND);
+        if (line_thr && tile == 0) ztc_store_a<NZ>(row, tmem + lane + ZTail<NZ>::COL_A);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) ztc_issue<NZ>(tmem, pieces, mbar);
+        if (line_thr) {
+            /* tile 0: band while the tail runs, then the tail; tile 1: its
+             * operand once tile 0's products have read theirs */
+            if (tile == 0) ztc_band<NZ>(row, bt);
+            /* warp-uniform: the TMEM accesses below are warp-collective */
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(mbar, ncommit & 1));
+            tc_fence_after();
+            if (!ok) *fault_flag = 1;
+            if (tile == 0) {
+                if (ok) ztc_combine<NZ>(row, tmem + lane);
+            } else if (ok) {
+                ztc_store_a<NZ>(row, tmem + lane + ZTail<NZ>::COL_A);
+            }
+        }
+        ++ncommit;
+        if constexpr (NTILE > 1) {
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) ztc_issue<NZ>(tmem, pieces, mbar);
+            if (line_thr && tile == 1) {
+                ztc_band<NZ>(row, bt);
+                const bool ok = __all_sync(0xffffffffu, mbar_wait(mbar, ncommit & 1));
+                tc_fence_after();
+                if (ok)
+                    ztc_combine<NZ>(row, tmem + lane);
+                else
+                    *fault_flag = 1;
+            }
+            ++ncommit;
+        }
+        tc_fence_before();
+    } else if constexpr (sizeof(P) == 4 && SCFT_F32X2 && (NZ / 2) % 8 == 0) {
         z_split2<NX, NZ, TM>(reinterpret_cast<float *>(X), reinterpret_cast<const float *>(KA),
                          reinterpret_cast<const float *>(KB), tid);
     } else {
@@ -608,6 +947,18 @@ __global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
         }
     }
     __syncthreads();
+    /* a tensor-core wait that gave up: this step's slice goes out as NaN (the
+     * instance then reports a non-finite status) and the chain stops */
+    bool stop_chain = false;
+    if constexpr (ZTC) {
+        tc_fence_after();
+        stop_chain = *fault_flag != 0;
+        if (stop_chain) {
+            if (tid == 0) atomicExch(&g_scft_tc_fault, 1);
+            for (int e = tid; e < NX * ZP; e += T) X[e] = __int_as_float(0x7fc00000);
+            __syncthreads();
+        }
+    }
     /* q_{s+1} = b . y to HBM for the densities; the next step's input
      * b_next . q_{s+1} stays in shared memory (b_next differs from b only at the
      * diblock junction), so b is read once per step. Each thread issues all of
@@ -679,7 +1030,19 @@ __global__ void __launch_bounds__(NX * TM) k_chain2d(Step2DArgs a)
         }
     }
     __syncthreads();
+    if (stop_chain) break;
     } /* contour steps */
+    if constexpr (ZTC) {
+        /* every TMEM access of this CTA has completed (waited loads, and the
+         * barrier above); the allocating warp frees the columns */
+        tc_fence_before();
+        __syncthreads();
+        if (tid < 32) {
+            tc_fence_after();
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"(ZTail<NZ>::TCOLS)
+                         : "memory");
+        }
+    }
 }
 
 /* ---------------------------------------------------------------- dispatch */
@@ -687,6 +1050,34 @@ template <typename P, int NX, int NZ, int N1, int N2>
 static size_t smem_bytes_t()
 {
     return Smem2D<P, NX, NZ>::END;
+}
+
+/* Dynamic shared memory of a launch. With the tensor-core z tail every CTA
+ * holds TCOLS of the SM's 512 TMEM columns for its whole chain, so the request
+ * is raised until no more CTAs fit on an SM than the columns serve: a CTA never
+ * waits in tcgen05.alloc for another chain to end. */
+template <typename P, int NX, int NZ, int N1, int N2>
+static size_t smem_launch_t()
+{
+    static size_t cached = 0;
+    if (cached) return cached;
+    size_t s = Smem2D<P, NX, NZ>::END;
+    if constexpr (Smem2D<P, NX, NZ>::TC) {
+        const int maxc = 512 / ZTail<NZ>::TCOLS;
+        int dev = 0, per_sm = 0, resv = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 233472;
+            resv = 1024;
+        }
+        /* (maxc + 1) CTAs of s + resv bytes each must not fit */
+        const long need = (long)per_sm / (maxc + 1) - resv + 16;
+        if (need > (long)s) s = (size_t)(need + 15) / 16 * 16;
+    }
+    cached = s;
+    return s;
 }
 
 /* Two threads per line where the z phase is the split one (NZ/2 a multiple of 8). */
@@ -698,7 +1089,7 @@ struct WideOk {
 template <typename P, int NX, int NZ, int N1, int N2>
 static cudaError_t launch_t(const Step2DArgs &a, int nblocks, cudaStream_t st, int configure, int wide)
 {
-    const size_t smem = smem_bytes_t<P, NX, NZ, N1, N2>();
+    const size_t smem = smem_launch_t<P, NX, NZ, N1, N2>();
     if (configure) {
         cudaError_t e = cudaFuncSetAttribute(k_chain2d<P, NX, NZ, N1, N2, 1>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -744,6 +1135,19 @@ size_t scft_step2d_smem(int prec, int nx, int nz)
     return 0;
 }
 
+/* 1 if the fused FP32 loop of (nx, nz) applies the z operator as an FP32 band
+ * plus a tensor-core tail (its operator table is then the band coefficients
+ * and the bf16 pieces, not the FP32 halves). */
+int scft_step2d_ztc(int prec, int nx, int nz)
+{
+    if (prec == SCFT_PREC_FP64) return 0;
+#define X(NX_, NZ_, A_, B_) \
+    if (nx == NX_ && nz == NZ_) return ZTcOk<float, NX_, NZ_>::value ? 1 : 0;
+    SCFT_STEP2D_SHAPES(X)
+#undef X
+    return 0;
+}
+
 /* 1 if the shape has the two-threads-per-line kernel (bit-identical results,
  * for batches of at most one chain per SM). */
 int scft_step2d_wide(int prec, int nx, int nz)
@@ -769,6 +1173,18 @@ cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, in
     SCFT_STEP2D_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
+}
+
+int scft_step2d_take_fault(void)
+{
+    int v = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_scft_tc_fault, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (v) cudaMemcpyToSymbol(g_scft_tc_fault, &zero, sizeof(int));
+    return v;
 }
 
 /* N1 of the four-step factorisation NX = N1 * N2 used for shape nx. */
