@@ -312,111 +312,172 @@ static long double bf16_val(uint16_t b)
 }
 
 /* Table of the tensor-core z operator of the fused FP32 2D loop (see
- * scft_step2d.cu): y = Kb x + Kt x with Kb the band |j - k| <= 3 of K (circular
- * for a periodic axis) and Kt = K - Kb.
- *   bytes [0, 32 nz): float band[nz][8], slot d + 3 of row j multiplying
- *     x[(j + d) mod nz], zero where a Dirichlet row has no such neighbour;
- *   then the tail's centrosymmetric halves Ae = (Kt[i][k] + Kt[i][nz-1-k]) / 2,
- *     Ao = (Kt[i][k] - Kt[i][nz-1-k]) / 2 (i, k < h), each split into bf16
- *     pieces hi = rn(A), lo = rn(A - hi), stored Ae.hi, Ae.lo, Ao.hi, Ao.lo as
- *     K-major 8 x 16-byte core matrices (element (i, k) at byte
- *     (i/8) 16h + (k/8) 128 + (i%8) 16 + (k%8) 2).
- * The band is rounded to FP32 so that every column sum of the operator the
- * kernel applies (FP32 band plus the bf16 pieces' sums) equals the column sum
- * of K as closely as FP32 allows, largest band entries moved first by one ulp
- * at most (the reasoning of round_fp32_colsum: no systematic per-step gain of
- * the dominant mode). */
+ * scft_step2d.cu): y = Kb x + Kt x, with Kb a band |j - k| <= 3 (circular for a
+ * periodic axis) in FP32 and Kt = K - Kb.
+ *   Band: the R0 = 8 rows at either end keep their own FP32 entries of K;
+ *   every interior row uses the same four constants c_d = K[h][h+d] (d = 0..3,
+ *   c_-d = c_d, h = nz/2), the Toeplitz part of K. Everything else, including
+ *   the interior rows' small Hankel parts near the diagonal and the FP32
+ *   rounding residuals of the band, is in the tail.
+ *   Tail: centrosymmetric halves Ae = (T[i][k] + T[i][nz-1-k]) / 2,
+ *   Ao = (T[i][k] - T[i][nz-1-k]) / 2 of the top rows (i, k < h), each split
+ *   into bf16 pieces hi = rn(A), lo = rn(A - hi). Column sums of the operator
+ *   the kernel applies (FP32 band plus the pieces' sums) are made equal to
+ *   those of K by moving Ae's diagonal: the mean mode passes through the
+ *   column sums, so no systematic per-step gain builds up over a chain.
+ * The bottom rows are the mirror images of the top rows (K is centrosymmetric).
+ * Layout (bytes): float band[2 R0][8] (rows 0..R0-1, then nz-R0..nz-1; slot
+ * d + 3 multiplies x[(j + d) mod nz], zero where a Dirichlet row has no such
+ * neighbour), float interior[8] = {c0, c1, c2, c3, 0...}, then Ae.hi, Ae.lo,
+ * Ao.hi, Ao.lo as K-major 8 x 16-byte core matrices (element (i, k) at byte
+ * (i/8) 16h + (k/8) 128 + (i%8) 16 + (k%8) 2 of its piece). */
 static std::vector<unsigned char> ztc_table(const std::vector<long double> &K, int nz, int periodic)
 {
-    const int h = nz / 2;
-    auto inband = [&](int j, int k) {
-        int d = j > k ? j - k : k - j;
-        if (periodic && nz - d < d) d = nz - d;
-        return d <= 3;
+    const int h = nz / 2, R0 = 8;
+    auto at = [&](int j, int k) { return K[(size_t)j * nz + k]; };
+    float cT[4];
+    for (int d = 0; d < 4; ++d) cT[d] = (float)((at(h, h + d) + at(h, h - d)) / 2.0L);
+    /* FP32 band value of top row i (< h) at column k, 0 off the band */
+    auto band = [&](int i, int k) -> float {
+        int d = k - i;
+        if (periodic) {
+            if (d > nz / 2) d -= nz;
+            if (d < -nz / 2) d += nz;
+        }
+        if (d < -3 || d > 3) return 0.0f;
+        if (i < R0) return (float)at(i, k);
+        return cT[d < 0 ? -d : d];
     };
-    std::vector<long double> T(K);
-    for (int j = 0; j < nz; ++j)
-        for (int k = 0; k < nz; ++k)
-            if (inband(j, k)) T[(size_t)j * nz + k] = 0.0L;
-    std::vector<uint16_t> pc((size_t)4 * h * h);
-    std::vector<long double> Aeff((size_t)h * h), Oeff((size_t)h * h);
+    std::vector<long double> Ae((size_t)h * h), Ao((size_t)h * h);
     for (int i = 0; i < h; ++i)
         for (int k = 0; k < h; ++k) {
-            const long double a = T[(size_t)i * nz + k], m = T[(size_t)i * nz + (nz - 1 - k)];
-            const long double ae = (a + m) / 2.0L, ao = (a - m) / 2.0L;
-            const uint16_t e1 = bf16_rn(ae), e2 = bf16_rn(ae - bf16_val(e1));
-            const uint16_t o1 = bf16_rn(ao), o2 = bf16_rn(ao - bf16_val(o1));
-            const size_t at = (size_t)i * h + k;
-            pc[0 * (size_t)h * h + at] = e1;
-            pc[1 * (size_t)h * h + at] = e2;
-            pc[2 * (size_t)h * h + at] = o1;
-            pc[3 * (size_t)h * h + at] = o2;
-            Aeff[at] = bf16_val(e1) + bf16_val(e2);
-            Oeff[at] = bf16_val(o1) + bf16_val(o2);
+            const long double t1 = at(i, k) - (long double)band(i, k);
+            const long double t2 = at(i, nz - 1 - k) - (long double)band(i, nz - 1 - k);
+            Ae[(size_t)i * h + k] = (t1 + t2) / 2.0L;
+            Ao[(size_t)i * h + k] = (t1 - t2) / 2.0L;
         }
-    /* the tail the kernel applies, in full form, and the FP32 band */
-    std::vector<long double> Teff((size_t)nz * nz, 0.0L);
-    for (int i = 0; i < h; ++i)
-        for (int k = 0; k < h; ++k) {
-            const long double ae = Aeff[(size_t)i * h + k], ao = Oeff[(size_t)i * h + k];
-            Teff[(size_t)i * nz + k] = ae + ao;
-            Teff[(size_t)i * nz + (nz - 1 - k)] = ae - ao;
-            Teff[(size_t)(nz - 1 - i) * nz + k] = ae - ao;
-            Teff[(size_t)(nz - 1 - i) * nz + (nz - 1 - k)] = ae + ao;
-        }
-    std::vector<float> B((size_t)nz * nz, 0.0f);
-    std::vector<int> rows;
-    for (int k = 0; k < nz; ++k) {
-        long double target = 0.0L, have = 0.0L;
-        rows.clear();
-        for (int j = 0; j < nz; ++j) {
-            target += K[(size_t)j * nz + k];
-            have += Teff[(size_t)j * nz + k];
-            if (inband(j, k)) {
-                const float r = (float)K[(size_t)j * nz + k];
-                B[(size_t)j * nz + k] = r;
-                have += (long double)r;
-                rows.push_back(j);
-            }
-        }
-        std::sort(rows.begin(), rows.end(), [&](int x, int y) {
-            return fabsl(K[(size_t)x * nz + k]) > fabsl(K[(size_t)y * nz + k]);
-        });
-        long double resid = target - have;
-        for (int j : rows) {
-            if (resid == 0.0L) break;
-            const float r = B[(size_t)j * nz + k];
-            if (r == 0.0f) continue;
-            const float up = nextafterf(r, INFINITY), dn = nextafterf(r, -INFINITY);
-            const long double ulp_up = (long double)up - r, ulp_dn = (long double)r - dn;
-            if (resid >= ulp_up / 2) {
-                B[(size_t)j * nz + k] = up;
-                resid -= ulp_up;
-            } else if (-resid >= ulp_dn / 2) {
-                B[(size_t)j * nz + k] = dn;
-                resid += ulp_dn;
-            }
-        }
+    std::vector<uint16_t> e1((size_t)h * h), e2((size_t)h * h), o1((size_t)h * h), o2((size_t)h * h);
+    auto split = [](long double v, uint16_t &p, uint16_t &q) {
+        p = bf16_rn(v);
+        q = bf16_rn(v - bf16_val(p));
+    };
+    for (size_t u = 0; u < (size_t)h * h; ++u) {
+        split(Ae[u], e1[u], e2[u]);
+        split(Ao[u], o1[u], o2[u]);
     }
-    const size_t nb = (size_t)32 * nz, piece = (size_t)2 * h * h;
-    std::vector<unsigned char> out(nb + 4 * piece, 0);
-    float *band = reinterpret_cast<float *>(out.data());
-    for (int j = 0; j < nz; ++j)
-        for (int d = -3; d <= 3; ++d) {
-            int k = j + d;
-            if (k < 0 || k >= nz) {
-                if (!periodic) continue;
-                k = (k + nz) % nz;
-            }
-            band[(size_t)j * 8 + (d + 3)] = B[(size_t)j * nz + k];
+    /* column sums (k < h; column nz-1-k is its mirror): K against FP32 band +
+     * 2 sum_i (Ae.hi + Ae.lo)[i][k]. The difference first goes onto Ae[k][k];
+     * what its bf16 pair cannot hold is then handed out one ulp of a lo piece
+     * at a time, largest entries first (at most one ulp per piece and pass). */
+    auto colsum_resid = [&](int k) {
+        long double target = 0.0L, have = 0.0L;
+        for (int i = 0; i < h; ++i) {
+            target += at(i, k) + at(i, nz - 1 - k);
+            have += (long double)band(i, k) + (long double)band(i, nz - 1 - k);
+            const size_t u = (size_t)i * h + k;
+            have += 2.0L * (bf16_val(e1[u]) + bf16_val(e2[u]));
         }
+        return target - have;
+    };
+    auto bf16_step = [](uint16_t b, int up) -> uint16_t { /* next bf16 toward +inf (up) or -inf */
+        const bool neg = (b & 0x8000u) != 0;
+        return (uint16_t)((up != neg) ? b + 1 : b - 1);
+    };
+    std::vector<int> order(h);
+    for (int k = 0; k < h; ++k) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const size_t u = (size_t)k * h + k;
+            Ae[u] += colsum_resid(k) / 2.0L;
+            split(Ae[u], e1[u], e2[u]);
+        }
+        for (int i = 0; i < h; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) {
+            return fabsl(Ae[(size_t)x * h + k]) > fabsl(Ae[(size_t)y * h + k]);
+        });
+        long double resid = colsum_resid(k);
+        for (int pass = 0; pass < 8 && resid != 0.0L; ++pass)
+            for (int i : order) {
+                uint16_t &q = e2[(size_t)i * h + k];
+                const long double v = bf16_val(q);
+                if (v == 0.0L || (q & 0x7f80u) == 0x7f80u) continue;
+                const uint16_t up = bf16_step(q, 1), dn = bf16_step(q, 0);
+                const long double du = bf16_val(up) - v, dd = v - bf16_val(dn);
+                if (resid >= du) {
+                    q = up;
+                    resid -= 2.0L * du;
+                } else if (-resid >= dd) {
+                    q = dn;
+                    resid += 2.0L * dd;
+                }
+            }
+    }
+    const size_t nb = (size_t)32 * (2 * R0 + 1), piece = (size_t)2 * h * h;
+    std::vector<unsigned char> out(nb + 4 * piece, 0);
+    float *bt = reinterpret_cast<float *>(out.data());
+    for (int r = 0; r < R0; ++r)
+        for (int d = -3; d <= 3; ++d) {
+            int k = r + d;
+            if (k < 0) {
+                if (!periodic) continue;
+                k += nz;
+            }
+            const float v = band(r, k);
+            bt[(size_t)r * 8 + (d + 3)] = v;                 /* top row r */
+            bt[(size_t)(2 * R0 - 1 - r) * 8 + (3 - d)] = v;  /* its mirror, row nz-1-r */
+        }
+    for (int d = 0; d < 4; ++d) bt[(size_t)2 * R0 * 8 + d] = cT[d];
+    const std::vector<uint16_t> *pcs[4] = {&e1, &e2, &o1, &o2};
     for (int p = 0; p < 4; ++p)
         for (int i = 0; i < h; ++i)
             for (int k = 0; k < h; ++k) {
                 const size_t off = nb + p * piece + (size_t)(i / 8) * 16 * h + (size_t)(k / 8) * 128 + (i % 8) * 16 + (k % 8) * 2;
-                memcpy(out.data() + off, &pc[(size_t)p * h * h + (size_t)i * h + k], 2);
+                memcpy(out.data() + off, &(*pcs[p])[(size_t)i * h + k], 2);
             }
     return out;
+}
+
+/* Test hook, not part of the ABI: the z operator that the tensor-core form of
+ * the fused 2D loop applies, decoded from its table the way the kernel reads
+ * it (k_eff, nz x nz row-major), next to the exact operator (k_ref). */
+extern "C" int scft_ztc_operator(int nz, double alpha, int dirichlet, double *k_eff, double *k_ref)
+{
+    if (nz < 32 || nz % 32 != 0 || !k_eff || !k_ref) return SCFT_ERR_PARAM;
+    const int h = nz / 2, R0 = 8;
+    std::vector<long double> K;
+    dense_operator(nz, alpha, dirichlet, K);
+    const std::vector<unsigned char> t = ztc_table(K, nz, !dirichlet);
+    const float *bt = reinterpret_cast<const float *>(t.data());
+    std::vector<long double> E((size_t)nz * nz, 0.0L);
+    for (int j = 0; j < nz; ++j)
+        for (int d = -3; d <= 3; ++d) {
+            float c;
+            if (j < R0)
+                c = bt[(size_t)j * 8 + d + 3];
+            else if (j >= nz - R0)
+                c = bt[(size_t)(j - nz + 2 * R0) * 8 + d + 3];
+            else
+                c = bt[(size_t)2 * R0 * 8 + (d < 0 ? -d : d)];
+            E[(size_t)j * nz + (j + d + nz) % nz] += (long double)c;
+        }
+    const size_t nb = (size_t)32 * (2 * R0 + 1), piece = (size_t)2 * h * h;
+    auto pc = [&](int p, int i, int k) {
+        uint16_t b;
+        memcpy(&b, t.data() + nb + p * piece + (size_t)(i / 8) * 16 * h + (size_t)(k / 8) * 128 + (i % 8) * 16 + (k % 8) * 2, 2);
+        return bf16_val(b);
+    };
+    for (int i = 0; i < h; ++i)
+        for (int k = 0; k < h; ++k) {
+            const long double ae = pc(0, i, k) + pc(1, i, k), ao = pc(2, i, k) + pc(3, i, k);
+            E[(size_t)i * nz + k] += ae + ao;
+            E[(size_t)i * nz + (nz - 1 - k)] += ae - ao;
+            E[(size_t)(nz - 1 - i) * nz + k] += ae - ao;
+            E[(size_t)(nz - 1 - i) * nz + (nz - 1 - k)] += ae + ao;
+        }
+    for (size_t u = 0; u < (size_t)nz * nz; ++u) {
+        k_eff[u] = (double)E[u];
+        k_ref[u] = (double)K[u];
+    }
+    return SCFT_OK;
 }
 
 /* z operator halves and x factor of one operator set for the fused 2D step. */

@@ -31,11 +31,16 @@
  */
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "scft_internal.h"
 
 /* Build switches of the fused chain kernel. */
 #ifndef SCFT_F32X2
 #define SCFT_F32X2 1 /* packed f32x2 FMA in the z phase */
+#endif
+#ifndef SCFT_BRES
+#define SCFT_BRES 1 /* store-phase items whose Boltzmann factors stay in registers */
 #endif
 #ifndef SCFT_ZROWS
 #define SCFT_ZROWS 2 /* output rows per pass of the packed z phase (2 or 4; measured equal) */
@@ -96,7 +101,8 @@ struct ZTail {
     static constexpr int PIECE = 2 * H * H;      /* bytes of one H x H bf16 operator piece */
     static constexpr int SBO = 16 * H;           /* bytes between 8-row core-matrix groups */
     static constexpr int LBO = 128;              /* bytes between K-adjacent core matrices */
-    static constexpr int BAND = 8;               /* band coefficients per output row (7 used) */
+    static constexpr int R0 = 8;                 /* rows at either end with their own band coefficients */
+    static constexpr int BAND_BYTES = 32 * (2 * R0 + 1); /* float[2 R0][8] + the interior constants float[8] */
 };
 
 /* byte offsets of the shared-memory regions: X, KA, KB, TW, EX; with the
@@ -112,7 +118,7 @@ struct Smem2D {
     static constexpr size_t TW = align16(KB + sizeof(P) * H * H);
     static constexpr size_t EX = align16(TW + 2 * sizeof(P) * NX);
     static constexpr size_t BAND = align16(EX + sizeof(P) * NX);
-    static constexpr size_t MBAR = TC ? align16(BAND + sizeof(float) * NZ * ZTail<NZ>::BAND) : BAND;
+    static constexpr size_t MBAR = TC ? align16(BAND + ZTail<NZ>::BAND_BYTES) : BAND;
     static constexpr size_t END = TC ? align16(MBAR + 16) : BAND;
     static_assert(!TC || 8 * H * H == KB - KA + sizeof(P) * H * H, "the bf16 pieces fill KA and KB");
 };
@@ -501,40 +507,51 @@ __device__ __forceinline__ void ztc_store_a(const float *row, uint32_t ta)
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-/* One thread issues the tail products of one tile and commits them to mb. */
-template <int NZ>
+/* One thread issues the tail products of one half of one tile (HALF 0: Pe =
+ * U Ae^T, HALF 1: Po = V Ao^T) and commits them to mb (two arrivals per tile). */
+template <int NZ, int HALF>
 __device__ __forceinline__ void ztc_issue(uint32_t tmem, uint32_t pieces, uint32_t mb)
 {
     using Z = ZTail<NZ>;
     constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(Z::H >> 3) << 17) | (8u << 24);
+    const uint32_t d = tmem + (HALF ? Z::COL_PO : Z::COL_PE);
+    const uint32_t p1 = pieces + (HALF ? 2 : 0) * Z::PIECE, p2 = p1 + Z::PIECE;
 #pragma unroll
     for (int c = 0; c < Z::H / 16; ++c) {
-        const uint32_t acc0 = c > 0;
-        const uint32_t aU1 = tmem + Z::COL_A + 8 * c, aU2 = aU1 + Z::PC, aV1 = aU1 + 2 * Z::PC, aV2 = aU1 + 3 * Z::PC;
-        const uint32_t off = 256u * c;
-        const uint64_t e1 = smem_desc(pieces + 0 * Z::PIECE + off, Z::LBO, Z::SBO);
-        const uint64_t e2 = smem_desc(pieces + 1 * Z::PIECE + off, Z::LBO, Z::SBO);
-        const uint64_t o1 = smem_desc(pieces + 2 * Z::PIECE + off, Z::LBO, Z::SBO);
-        const uint64_t o2 = smem_desc(pieces + 3 * Z::PIECE + off, Z::LBO, Z::SBO);
-        mma_bf16(tmem + Z::COL_PE, aU2, e1, IDESC, acc0);
-        mma_bf16(tmem + Z::COL_PE, aU1, e2, IDESC, 1u);
-        mma_bf16(tmem + Z::COL_PE, aU1, e1, IDESC, 1u);
-        mma_bf16(tmem + Z::COL_PO, aV2, o1, IDESC, acc0);
-        mma_bf16(tmem + Z::COL_PO, aV1, o2, IDESC, 1u);
-        mma_bf16(tmem + Z::COL_PO, aV1, o1, IDESC, 1u);
+        const uint32_t a1 = tmem + Z::COL_A + (HALF ? 2 : 0) * Z::PC + 8 * c, a2 = a1 + Z::PC;
+        const uint64_t k1 = smem_desc(p1 + 256u * c, Z::LBO, Z::SBO);
+        const uint64_t k2 = smem_desc(p2 + 256u * c, Z::LBO, Z::SBO);
+        mma_bf16(d, a2, k1, IDESC, c > 0 ? 1u : 0u);
+        mma_bf16(d, a1, k2, IDESC, 1u);
+        mma_bf16(d, a1, k1, IDESC, 1u);
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
 }
 
-/* Band part of one line, written over the line in place: coefficient slot
- * d + 3 of row j multiplies x[(j + d) mod NZ] (zero where a Dirichlet row has
- * no such neighbour); small terms first. A window x[j-3 .. j+5] moves along
- * the line in registers, so every value is read before its slot is written;
- * the last two pairs wrap to the saved head of the line. */
+/* The two halves of a tile's tail, issued by lane 0 of warps w0 and w0 + 1
+ * (idle warps where there are any; a CTA of one warp issues both). */
+template <int NZ, int T>
+__device__ __forceinline__ void ztc_issue_tile(int tid, int w0, uint32_t tmem, uint32_t pieces, uint32_t mb)
+{
+    if (tid == 32 * w0) ztc_issue<NZ, 0>(tmem, pieces, mb);
+    if (tid == (T > 32 ? 32 * (w0 + 1) : 0)) ztc_issue<NZ, 1>(tmem, pieces, mb);
+}
+
+/* Band part of one line, written over the line in place. The R0 rows at
+ * either end have their own coefficients (slot d + 3 of table row r multiplies
+ * x[(j + d) mod NZ], zero where a Dirichlet row has no such neighbour); every
+ * interior row applies the symmetric constants c0..c3:
+ * y = c0 x_j + c1 (x_j-1 + x_j+1) + c2 (x_j-2 + x_j+2) + c3 (x_j-3 + x_j+3),
+ * small terms first. A window x[j-3 .. j+5] moves along the line in registers,
+ * so every value is read before its slot is written; the last two pairs wrap
+ * to the saved head of the line. */
 template <int NZ>
 __device__ __forceinline__ void ztc_band(float *row, const float *bt)
 {
+    constexpr int R0 = ZTail<NZ>::R0;
+    static_assert(NZ >= 2 * R0 + 8 && R0 % 2 == 0, "interior rows between the end rows");
     const float4 *b4 = reinterpret_cast<const float4 *>(bt);
+    const float4 cc = b4[4 * R0]; /* c0, c1, c2, c3 */
     const float2 h01 = *reinterpret_cast<const float2 *>(row);
     const float2 h23 = *reinterpret_cast<const float2 *>(row + 2);
     const float2 t0 = *reinterpret_cast<const float2 *>(row + NZ - 4);
@@ -548,11 +565,16 @@ __device__ __forceinline__ void ztc_band(float *row, const float *bt)
     w[4] = head[1];
     w[5] = head[2];
     w[6] = head[3];
-    auto pair = [&](int j) {
+    auto shift = [&]() {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) w[i] = w[i + 2];
+    };
+    /* rows j, j+1 with their own coefficients (table rows r, r+1) */
+    auto pair_rows = [&](int j, int r) {
         float y[2];
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
-            const float4 ca = b4[2 * (j + e)], cb = b4[2 * (j + e) + 1];
+            const float4 ca = b4[2 * (r + e)], cb = b4[2 * (r + e) + 1];
             const float *x = w + e; /* x[d + 3] = x_{j+e+d} */
             float t = ca.x * x[0];
             t = fmaf(cb.z, x[6], t);
@@ -563,22 +585,49 @@ __device__ __forceinline__ void ztc_band(float *row, const float *bt)
             y[e] = fmaf(ca.w, x[3], t);
         }
         *reinterpret_cast<float2 *>(row + j) = make_float2(y[0], y[1]);
-#pragma unroll
-        for (int i = 0; i < 7; ++i) w[i] = w[i + 2];
     };
+    auto pair_const = [&](int j) {
+        float y[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float *x = w + e;
+            float t = cc.w * (x[0] + x[6]);
+            t = fmaf(cc.z, x[1] + x[5], t);
+            t = fmaf(cc.y, x[2] + x[4], t);
+            y[e] = fmaf(cc.x, x[3], t);
+        }
+        *reinterpret_cast<float2 *>(row + j) = make_float2(y[0], y[1]);
+    };
+    auto next = [&](int j) { /* x[j+4], x[j+5] into the window */
+        if (j + 4 < NZ) {
+            const float2 n = *reinterpret_cast<const float2 *>(row + j + 4);
+            w[7] = n.x;
+            w[8] = n.y;
+        } else {
+            w[7] = head[j + 4 - NZ];
+            w[8] = head[j + 5 - NZ];
+        }
+    };
+#pragma unroll
+    for (int j = 0; j < R0; j += 2) {
+        next(j);
+        pair_rows(j, j);
+        shift();
+    }
 #pragma unroll 4
-    for (int j = 0; j < NZ - 4; j += 2) {
+    for (int j = R0; j < NZ - R0; j += 2) {
         const float2 n = *reinterpret_cast<const float2 *>(row + j + 4);
         w[7] = n.x;
         w[8] = n.y;
-        pair(j);
+        pair_const(j);
+        shift();
     }
-    w[7] = head[0];
-    w[8] = head[1];
-    pair(NZ - 4);
-    w[7] = head[2];
-    w[8] = head[3];
-    pair(NZ - 2);
+#pragma unroll
+    for (int j = NZ - R0; j < NZ; j += 2) {
+        next(j);
+        pair_rows(j, j - NZ + 2 * R0);
+        shift();
+    }
 }
 
 /* Adds the tail (Pe + Po on top, Pe - Po mirrored below) to the band values of
@@ -671,8 +720,8 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
         constexpr int VP = 16 / sizeof(P);
         const P *gA = reinterpret_cast<const P *>(cd.ops->kz);
         if constexpr (ZTC) {
-            /* band coefficients [NZ][8] FP32, then the four bf16 pieces (8 H^2 bytes) */
-            constexpr int NB = NZ * ZTail<NZ>::BAND / 4, NP = 8 * H * H / 16;
+            /* band coefficients (FP32), then the four bf16 pieces (8 H^2 bytes) */
+            constexpr int NB = ZTail<NZ>::BAND_BYTES / 16, NP = 8 * H * H / 16;
             const unsigned char *g = reinterpret_cast<const unsigned char *>(gA);
             for (int e = tid; e < NB; e += T) cp_async16(smem_raw + L::BAND + 16 * e, g + 16 * e);
             for (int e = tid; e < NP; e += T) cp_async16(smem_raw + L::KA + 16 * e, g + 16 * NB + 16 * e);
@@ -705,7 +754,7 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
     if constexpr (ZTC) {
         const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(smem_raw + L::MBAR);
         if (tid == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(mbar) : "memory");
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             *fault_flag = 0;
         }
@@ -739,6 +788,13 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
         }
     }
     __syncthreads();
+
+    /* the Boltzmann factor of a chain segment is the same slice at every step:
+     * each thread keeps its values for its first RES store-phase items in
+     * registers from step to step (reloaded at the diblock junction) */
+    constexpr int RES = FUSE_A ? (ITEMS < SCFT_BRES ? ITEMS : SCFT_BRES) : 0;
+    T2 bres[RES > 0 ? RES * N1 : 1];
+    const void *bres_src = nullptr;
 
     for (int s = a.s; s < s_end; ++s) {
     const P *bz = reinterpret_cast<const P *>(s < cd.seg_end ? cd.b0 : cd.b1);
@@ -819,7 +875,8 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        if (tid == 0) ztc_issue<NZ>(tmem, pieces, mbar);
+        /* tile 0's products: from the tile-1 warps, idle until they finish */
+        ztc_issue_tile<NZ, T>(tid, NTILE > 1 ? 4 : 0, tmem, pieces, mbar);
         if (line_thr) {
             /* tile 0: band while the tail runs, then the tail; tile 1: its
              * operand once tile 0's products have read theirs */
@@ -839,7 +896,7 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
             tc_fence_before();
             __syncthreads();
             tc_fence_after();
-            if (tid == 0) ztc_issue<NZ>(tmem, pieces, mbar);
+            ztc_issue_tile<NZ, T>(tid, 0, tmem, pieces, mbar);
             if (line_thr && tile == 1) {
                 ztc_band<NZ>(row, bt);
                 const bool ok = __all_sync(0xffffffffu, mbar_wait(mbar, ncommit & 1));
@@ -968,40 +1025,59 @@ __global__ void __launch_bounds__(NX * TM, (MinBlocks2D<P, NX, NZ, TM>::value)) 
     if (FUSE_A && s + 1 < s_end) {
         const T2 *b2p = reinterpret_cast<const T2 *>(bz);
         const T2 *n2p = reinterpret_cast<const T2 *>(bnext);
-        const bool same_b = (bnext == bz);
-        T2 bb[ITEMS * N1];
-#pragma unroll
-        for (int it = 0; it < ITEMS; ++it) {
+        /* the next step's factor differs only at the diblock junction: a
+         * separate body for that step keeps its extra loads out of every other */
+        auto load = [&](int it, T2 *dst) {
             const int w = tid + it * T, n2 = w / NZ2, c = w - n2 * NZ2;
             if (ITEMS_EVEN || w < N2 * NZ2) {
 #pragma unroll
-                for (int n1 = 0; n1 < N1; ++n1) bb[it * N1 + n1] = b2p[(N2 * n1 + n2) * NZ2 + c];
+                for (int n1 = 0; n1 < N1; ++n1) dst[n1] = b2p[(N2 * n1 + n2) * NZ2 + c];
             }
+        };
+        if (bres_src != bz) {
+#pragma unroll
+            for (int it = 0; it < RES; ++it) load(it, bres + it * N1);
+            bres_src = bz;
         }
+        auto store_items = [&](auto next_differs) {
+            constexpr bool NB = decltype(next_differs)::value;
+            /* items past the resident ones: loads one item ahead of their use */
+            T2 cur[N1], nxt[N1];
+            if (RES < ITEMS) load(RES, cur);
 #pragma unroll
-        for (int it = 0; it < ITEMS; ++it) {
-            const int w = tid + it * T, n2 = w / NZ2, c = w - n2 * NZ2;
-            if (!ITEMS_EVEN && w >= N2 * NZ2) break;
-            Cx<P> v[N1];
+            for (int it = 0; it < ITEMS; ++it) {
+                if (it >= RES && it + 1 < ITEMS) load(it + 1, nxt);
+                const int w = tid + it * T, n2 = w / NZ2, c = w - n2 * NZ2;
+                if (!ITEMS_EVEN && w >= N2 * NZ2) break;
+                Cx<P> v[N1];
 #pragma unroll
-            for (int n1 = 0; n1 < N1; ++n1) {
-                const int e = (N2 * n1 + n2) * NZ2 + c;
-                const T2 y = reinterpret_cast<const T2 *>(X)[(N2 * n1 + n2) * ZP2 + c];
-                const T2 bv = bb[it * N1 + n1];
-                T2 o;
-                o.x = y.x * bv.x;
-                o.y = y.y * bv.y;
-                reinterpret_cast<T2 *>(qn)[e] = o;
-                const T2 nb = same_b ? bv : n2p[e];
-                v[n1].x = o.x * nb.x;
-                v[n1].y = o.y * nb.y;
+                for (int n1 = 0; n1 < N1; ++n1) {
+                    const int e = (N2 * n1 + n2) * NZ2 + c;
+                    const T2 y = reinterpret_cast<const T2 *>(X)[(N2 * n1 + n2) * ZP2 + c];
+                    const T2 bv = it < RES ? bres[it * N1 + n1] : cur[n1];
+                    T2 o;
+                    o.x = y.x * bv.x;
+                    o.y = y.y * bv.y;
+                    reinterpret_cast<T2 *>(qn)[e] = o;
+                    const T2 nb = NB ? n2p[e] : bv;
+                    v[n1].x = o.x * nb.x;
+                    v[n1].y = o.y * nb.y;
+                }
+                Dft<P, N1, false>::run(v);
+#pragma unroll
+                for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], TW[n2 * N1 + k1]);
+#pragma unroll
+                for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
+                if (it >= RES) {
+#pragma unroll
+                    for (int n1 = 0; n1 < N1; ++n1) cur[n1] = nxt[n1];
+                }
             }
-            Dft<P, N1, false>::run(v);
-#pragma unroll
-            for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], TW[n2 * N1 + k1]);
-#pragma unroll
-            for (int k1 = 0; k1 < N1; ++k1) XC[(N2 * k1 + n2) * ZP2 + c] = v[k1];
-        }
+        };
+        if (bnext == bz)
+            store_items(std::false_type{});
+        else
+            store_items(std::true_type{});
     } else {
         static_assert(NZ2 % TM == 0, "pairs must split evenly over the threads");
         constexpr int PER = NZ2 / TM; /* pairs per thread */
