@@ -512,18 +512,18 @@ def run_reference(args, rank, world):
     srn = importlib.import_module(PKG)
     surfaces = workload_surfaces(srn, args.workload, args.batch)
     threads = args.cpu_threads or os.cpu_count() or 1
-    cpu_sample(surfaces, threads, 1) if args.warmup > 0 else None
-    rates = []
-    steps = min(args.steps, args.ref_max_steps)
+    warmup = args.warmup if args.ref_max_steps <= 0 else min(args.warmup, args.ref_max_steps)
+    steps = args.steps if args.ref_max_steps <= 0 else min(args.steps, args.ref_max_steps)
+    for _ in range(warmup):
+        cpu_sample(surfaces, threads, 1)
     t_all = 0.0
     for _ in range(steps):
-        r, wall = cpu_sample(surfaces, threads, 1)
-        rates.append(r)
+        _, wall = cpu_sample(surfaces, threads, 1)
         t_all += wall
     value = threads * steps / t_all
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "instance-iterations/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3 / steps,
+        "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": t_all * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": workload_data(args.workload),
         "config": workload_config(args, surfaces),
@@ -566,8 +566,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--e2e-parts", type=int, default=8, help="contexts the e2e batch is pipelined over")
     ap.add_argument("--cpu-threads", type=int, default=0)
-    ap.add_argument("--cpu-iters", type=int, default=1)
-    ap.add_argument("--ref-max-steps", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=5, help="iterations per host thread of the CPU baseline sample")
+    ap.add_argument("--ref-max-steps", type=int, default=0,
+                    help="cap on the reference arm's timed (and warm-up) steps; 0: run --steps as given")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--sweep-n", type=int, default=16, help="n x n chi points of the droplet sweep (0: skip)")

@@ -264,10 +264,14 @@ int scft_density(scft_ctx *ctx, const double *qf, const double *qb, int len, int
  * device synchronisation cudaMalloc/cudaFree may cause or an allocation failure
  * mid-run). Same arguments and result; the working buffers live in one fixed
  * device array of scft_static_scratch_bytes() bytes per GPU, held until exit.
- * The first call on a device looks up that array's address (make it before any
- * stream capture). Calls share the array: overlapping calls on one GPU race and
- * must be serialised by the caller. Sizes that do not fit return SCFT_ERR_PARAM
- * with a message in scft_last_error(). It has no counterpart in the reference. */
+ * The first call on a device looks up that array's address and keeps it, so
+ * the device must not be reset after that call. Every call synchronises its
+ * stream and copies to pageable host memory: it cannot be called inside a
+ * stream capture. Calls share the array: overlapping calls on one GPU race and
+ * must be serialised by the caller (each call returns only after its own GPU
+ * work has finished, on errors too). Sizes that do not fit return
+ * SCFT_ERR_PARAM with a message in scft_last_error(). It has no counterpart in
+ * the reference. */
 int scft_propagate_static(scft_ctx *ctx, const double *q0, const double *w, int steps, double *q_out);
 size_t scft_static_scratch_bytes(void);
 
@@ -297,6 +301,30 @@ const char *scft_last_error(void);
  * drand48 does after seed48. out: n_active * M doubles, [active field][idx].
  * out may be NULL to only advance the state (the reference draws even when MF=0). */
 int scft_noise_fill(unsigned short state[3], const scft_derived *d, double *out);
+
+/* File names of the text I/O: the file-name macros of parameters.h
+ * (parameters.h:181-190, opened by SCFT.c at :704, :756, :847, :869, :1026,
+ * :1585-1661). density is the prefix of the snapshot names (density +
+ * 100000000+iter + ".dat"). Names are relative to dir (or the cwd). */
+#define SCFT_NAME_MAX 256
+typedef struct scft_file_names {
+    char counter[SCFT_NAME_MAX];        /* COUNTER        "counter.dat" */
+    char density[SCFT_NAME_MAX];        /* DENSITY        "densities_dbk_" */
+    char deviations[SCFT_NAME_MAX];     /* DEVIATIONS     "deviations.dat" */
+    char energy[SCFT_NAME_MAX];         /* ENERGY         "energies.dat" */
+    char restart_fields[SCFT_NAME_MAX]; /* RESTART_FIELDS "restart_fields.dat" */
+    char restart_random[SCFT_NAME_MAX]; /* RESTART_RANDOM "restart_random.dat" */
+    char run_params[SCFT_NAME_MAX];     /* RUN_PARAMS     "run.txt" */
+    char w_mask[SCFT_NAME_MAX];         /* W_MASK         "wMask.dat" */
+    char free_energy[SCFT_NAME_MAX];    /* FREE_ENERGY    "free_energy.dat" */
+} scft_file_names;
+/* Fills n with the reference's default names. */
+void scft_file_names_default(scft_file_names *n);
+/* Sets the names every reader and writer below uses from now on, in this
+ * process (NULL restores the defaults). Empty or unterminated names return
+ * SCFT_ERR_PARAM. Not thread-safe against concurrent I/O calls: set the names
+ * once, before the run, as SCFT.c compiles them in. */
+int scft_set_file_names(const scft_file_names *n);
 
 /* Text I/O with the reference's exact formats. dir may be NULL for the cwd. */
 int scft_read_counter(const char *dir, unsigned long *iter);             /* SCFT.c:704-716 */

@@ -19,7 +19,9 @@ ORACLE = Path(__file__).resolve().parent
 BUILD = ORACLE / "_build"
 REF_OUT = ORACLE / "_ref"
 SHIM = ORACLE / "fftw_shim"
-REFERENCE_SRC = Path(os.environ.get("SCFT_REFERENCE_DIR", "/root/reference")) / "SCFT.c"
+#: the reference source tree comes only from the environment (SCFT_REFERENCE_DIR)
+REFERENCE_DIR = os.environ.get("SCFT_REFERENCE_DIR")
+REFERENCE_SRC = Path(REFERENCE_DIR) / "SCFT.c" if REFERENCE_DIR else None
 LIB = BUILD / "liboracle.so"
 
 CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-fno-fast-math", f"-I{SHIM}"]
@@ -42,10 +44,13 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def reference_available() -> bool:
-    return REFERENCE_SRC.exists()
+    return REFERENCE_SRC is not None and REFERENCE_SRC.exists()
 
 
 def build_reference(case_dir: Path, parameters_h: str, full_precision: bool = True, shared: bool = False) -> Path:
+    if not reference_available():
+        raise RuntimeError("the reference source tree is not available: set SCFT_REFERENCE_DIR to the directory "
+                           "holding SCFT.c")
     """Compile the unmodified SCFT.c against ``parameters_h`` inside case_dir.
 
     full_precision appends the fprintf redirect (ref_support/precise_fprintf.c)

@@ -11,7 +11,7 @@
  * of the drand48 noise. Each function cites the SCFT.c lines it follows.
  *
  * Parity is pinned against the reference itself: tests/golden holds outputs
- * of SCFT.c built from its own source (oracle/build_ref.py) on seeded inputs,
+ * of SCFT.c built from its own source (oracle/build.py) on seeded inputs,
  * and the oracle must reproduce them.
  */
 #include <complex.h>

@@ -98,6 +98,15 @@ class CBatchResult(C.Structure):
                 ("converged", C.c_int), ("status", C.c_int)]
 
 
+NAME_MAX = 256
+FILE_NAME_FIELDS = ["counter", "density", "deviations", "energy", "restart_fields", "restart_random", "run_params",
+                    "w_mask", "free_energy"]
+
+
+class CFileNames(C.Structure):
+    _fields_ = [(n, C.c_char * NAME_MAX) for n in FILE_NAME_FIELDS]
+
+
 class CTiming(C.Structure):
     _fields_ = [("total_ms", D), ("prop_ms", D), ("prop_launches", C.c_long), ("kernel_launches", C.c_long),
                 ("fused_chain", C.c_int), ("threads_per_line", C.c_int)]
@@ -174,6 +183,8 @@ def lib() -> C.CDLL:
         "scft_write_run_params": (I, [C.c_char_p, P(CSurface), P(CDerived), UL]),
         "scft_write_energies": (I, [C.c_char_p, P(CDerived), P(CIterOut)]),
         "scft_write_snapshot": (I, [C.c_char_p, P(CDerived), UL, dp, dp, us3]),
+        "scft_file_names_default": (None, [P(CFileNames)]),
+        "scft_set_file_names": (I, [P(CFileNames)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -14,6 +14,50 @@
 
 #include "scft_gpu.h"
 
+/* ---------------------------------------------------------- file names */
+void scft_file_names_default(scft_file_names *n)
+{
+    if (!n) return;
+    memset(n, 0, sizeof(*n));
+    strcpy(n->counter, "counter.dat");
+    strcpy(n->density, "densities_dbk_");
+    strcpy(n->deviations, "deviations.dat");
+    strcpy(n->energy, "energies.dat");
+    strcpy(n->restart_fields, "restart_fields.dat");
+    strcpy(n->restart_random, "restart_random.dat");
+    strcpy(n->run_params, "run.txt");
+    strcpy(n->w_mask, "wMask.dat");
+    strcpy(n->free_energy, "free_energy.dat");
+}
+
+static scft_file_names g_names;
+static int g_names_set;
+
+static const scft_file_names *names(void)
+{
+    if (!g_names_set) {
+        scft_file_names_default(&g_names);
+        g_names_set = 1;
+    }
+    return &g_names;
+}
+
+int scft_set_file_names(const scft_file_names *n)
+{
+    if (!n) {
+        scft_file_names_default(&g_names);
+        g_names_set = 1;
+        return SCFT_OK;
+    }
+    const char *all[9] = {n->counter, n->density, n->deviations, n->energy, n->restart_fields,
+                          n->restart_random, n->run_params, n->w_mask, n->free_energy};
+    for (int i = 0; i < 9; ++i)
+        if (!all[i][0] || memchr(all[i], 0, SCFT_NAME_MAX) == NULL) return SCFT_ERR_PARAM;
+    g_names = *n;
+    g_names_set = 1;
+    return SCFT_OK;
+}
+
 static FILE *open_in(const char *dir, const char *name, const char *mode)
 {
     char path[4096];
@@ -27,7 +71,7 @@ static FILE *open_in(const char *dir, const char *name, const char *mode)
 /* ------------------------------------------------------------- readers */
 int scft_read_counter(const char *dir, unsigned long *iter)
 {
-    FILE *f = open_in(dir, "counter.dat", "r");
+    FILE *f = open_in(dir, names()->counter, "r");
     if (!f) return SCFT_ERR_IO;
     int ok = fscanf(f, "%lu", iter) == 1;
     fclose(f);
@@ -36,7 +80,7 @@ int scft_read_counter(const char *dir, unsigned long *iter)
 
 int scft_read_restart_fields(const char *dir, const scft_derived *d, double *w14)
 {
-    FILE *f = open_in(dir, "restart_fields.dat", "r");
+    FILE *f = open_in(dir, names()->restart_fields, "r");
     if (!f) return SCFT_ERR_IO;
     const long M = d->m;
     int bad = 0;
@@ -53,7 +97,7 @@ int scft_read_restart_fields(const char *dir, const scft_derived *d, double *w14
 
 int scft_read_restart_random(const char *dir, unsigned short seed[3])
 {
-    FILE *f = open_in(dir, "restart_random.dat", "r");
+    FILE *f = open_in(dir, names()->restart_random, "r");
     if (!f) return SCFT_ERR_IO;
     int ok = fscanf(f, "%hu %hu %hu", &seed[0], &seed[1], &seed[2]) == 3;
     fclose(f);
@@ -62,7 +106,7 @@ int scft_read_restart_random(const char *dir, unsigned short seed[3])
 
 int scft_read_mask(const char *dir, const scft_derived *d, double *mask3)
 {
-    FILE *f = open_in(dir, "wMask.dat", "r");
+    FILE *f = open_in(dir, names()->w_mask, "r");
     if (!f) return SCFT_ERR_IO;
     const long M = d->m;
     int bad = 0;
@@ -91,7 +135,7 @@ static const char *const FNAME[SCFT_NFIELDS] = {"A", "B", "C", "D", "E", "F", "G
 int scft_write_run_params(const char *dir, const scft_surface *s, const scft_derived *d, unsigned long iter)
 {
     /* run.txt, appended at launch (SCFT.c:1025-1085). */
-    FILE *f = open_in(dir, "run.txt", "a");
+    FILE *f = open_in(dir, names()->run_params, "a");
     if (!f) return SCFT_ERR_IO;
     const double (*X)[SCFT_NFIELDS] = (const double (*)[SCFT_NFIELDS])d->chi_eff;
     fprintf(f, "-----------------------------------------\n\n");
@@ -139,17 +183,17 @@ int scft_write_energies(const char *dir, const scft_derived *d, const scft_iter_
 {
     /* SCFT.c:1585-1598: one line each in energies.dat, free_energy.dat and
      * deviations.dat (the last also echoes chi_AB, chi_AC, chi_BC EFF). */
-    FILE *f = open_in(dir, "energies.dat", "a");
+    FILE *f = open_in(dir, names()->energy, "a");
     if (!f) return SCFT_ERR_IO;
     fprintf(f, "%lu", o->iter);
     for (int sp = 0; sp < SCFT_NSPECIES; ++sp) fprintf(f, " %lf", o->mu[sp]);
     fprintf(f, "\n");
     fclose(f);
-    f = open_in(dir, "free_energy.dat", "a");
+    f = open_in(dir, names()->free_energy, "a");
     if (!f) return SCFT_ERR_IO;
     fprintf(f, "%lu  %lf  %f \n", o->iter, o->free_energy, (double)(float)o->mf);
     fclose(f);
-    f = open_in(dir, "deviations.dat", "a");
+    f = open_in(dir, names()->deviations, "a");
     if (!f) return SCFT_ERR_IO;
     fprintf(f, "%lu  %lf %lf %lf %lf \n", o->iter, o->rms, d->chi_eff[0][1], d->chi_eff[0][2], d->chi_eff[1][2]);
     fclose(f);
@@ -160,9 +204,9 @@ int scft_write_snapshot(const char *dir, const scft_derived *d, unsigned long it
                         const double *w14, const unsigned short seed[3])
 {
     const long M = d->m;
-    char name[64];
+    char name[SCFT_NAME_MAX + 32];
     /* densities_dbk_<100000000 + iIter>.dat (SCFT.c:1603-1610). */
-    snprintf(name, sizeof(name), "densities_dbk_%d.dat", (int)(100000000 + iter));
+    snprintf(name, sizeof(name), "%s%d.dat", names()->density, (int)(100000000 + iter));
     FILE *f = open_in(dir, name, "w");
     if (!f) return SCFT_ERR_IO;
     for (int k = 0; k < d->nz; ++k)
@@ -176,12 +220,12 @@ int scft_write_snapshot(const char *dir, const scft_derived *d, unsigned long it
             }
     fclose(f);
 
-    f = open_in(dir, "counter.dat", "w"); /* SCFT.c:1631-1634 */
+    f = open_in(dir, names()->counter, "w"); /* SCFT.c:1631-1634 */
     if (!f) return SCFT_ERR_IO;
     fprintf(f, "%lu", iter);
     fclose(f);
 
-    f = open_in(dir, "restart_fields.dat", "w"); /* SCFT.c:1636-1650 */
+    f = open_in(dir, names()->restart_fields, "w"); /* SCFT.c:1636-1650 */
     if (!f) return SCFT_ERR_IO;
     for (int k = 0; k < d->nz; ++k)
         for (int j = 0; j < d->ny; ++j)
@@ -193,7 +237,7 @@ int scft_write_snapshot(const char *dir, const scft_derived *d, unsigned long it
     fclose(f);
 
     if (seed) {
-        f = open_in(dir, "restart_random.dat", "w"); /* SCFT.c:1652-1663 */
+        f = open_in(dir, names()->restart_random, "w"); /* SCFT.c:1652-1663 */
         if (!f) return SCFT_ERR_IO;
         fprintf(f, "%hu %hu %hu", seed[0], seed[1], seed[2]);
         fclose(f);

@@ -13,8 +13,11 @@
  *
  * The FP64 plain form is the default; SCFT_GB300_PRECISION=fp32 selects the
  * FP32-propagator form. The drand48 noise stream is replayed on the device;
- * SCFT_GB300_NOISE=host draws it on the host instead (same numbers). The file-name macros of parameters.h are not read: the
- * files carry the reference's default names.
+ * SCFT_GB300_NOISE=host draws it on the host instead (same numbers). The
+ * file-name macros of parameters.h (COUNTER, DENSITY, DEVIATIONS, ENERGY,
+ * RESTART_FIELDS, RESTART_RANDOM, RUN_PARAMS, W_MASK, FREE_ENERGY;
+ * parameters.h:181-190) name the files as they do for SCFT.c; a header without
+ * them gets the reference's names.
  */
 #include <math.h>
 #include <stdio.h>
@@ -24,6 +27,54 @@
 
 #include "parameters.h"
 #include "scft_gpu.h"
+
+#ifndef COUNTER
+#define COUNTER "counter.dat"
+#endif
+#ifndef DENSITY
+#define DENSITY "densities_dbk_"
+#endif
+#ifndef DEVIATIONS
+#define DEVIATIONS "deviations.dat"
+#endif
+#ifndef ENERGY
+#define ENERGY "energies.dat"
+#endif
+#ifndef RESTART_FIELDS
+#define RESTART_FIELDS "restart_fields.dat"
+#endif
+#ifndef RESTART_RANDOM
+#define RESTART_RANDOM "restart_random.dat"
+#endif
+#ifndef RUN_PARAMS
+#define RUN_PARAMS "run.txt"
+#endif
+#ifndef W_MASK
+#define W_MASK "wMask.dat"
+#endif
+#ifndef FREE_ENERGY
+#define FREE_ENERGY "free_energy.dat"
+#endif
+
+/* the run's file names as SCFT.c compiles them in (parameters.h:181-190) */
+static void set_names(void)
+{
+    scft_file_names n;
+    memset(&n, 0, sizeof(n));
+    snprintf(n.counter, sizeof(n.counter), "%s", COUNTER);
+    snprintf(n.density, sizeof(n.density), "%s", DENSITY);
+    snprintf(n.deviations, sizeof(n.deviations), "%s", DEVIATIONS);
+    snprintf(n.energy, sizeof(n.energy), "%s", ENERGY);
+    snprintf(n.restart_fields, sizeof(n.restart_fields), "%s", RESTART_FIELDS);
+    snprintf(n.restart_random, sizeof(n.restart_random), "%s", RESTART_RANDOM);
+    snprintf(n.run_params, sizeof(n.run_params), "%s", RUN_PARAMS);
+    snprintf(n.w_mask, sizeof(n.w_mask), "%s", W_MASK);
+    snprintf(n.free_energy, sizeof(n.free_energy), "%s", FREE_ENERGY);
+    if (scft_set_file_names(&n) != SCFT_OK) {
+        fprintf(stderr, "invalid file names in parameters.h\n");
+        exit(EXIT_FAILURE);
+    }
+}
 
 #define CHI(f, g, v)                  \
     do {                              \
@@ -108,6 +159,7 @@ static void check(int rc, const char *what)
 
 int main(void)
 {
+    set_names();
     scft_surface S;
     surface_from_macros(&S);
     scft_derived d;

@@ -12,15 +12,22 @@
  *
  * Set-up: the device address of the array is looked up with
  * cudaGetSymbolAddress the first time the entry point runs on a device (with
- * that device current); make that first call before any stream capture.
- * Every call on a device reuses the same array and leaves the previous call's
- * data in it; each call writes every byte it later reads, so nothing needs to
- * start at zero. Calls that overlap on the GPU (other threads, other contexts on
- * the same device) race on the array and must be serialised by the caller.
+ * that device current) and kept for the life of the process, so a device reset
+ * (cudaDeviceReset, or the primary context torn down and created again) after
+ * that first call is not supported. The function synchronises its stream and
+ * copies into pageable host memory, so it cannot be called inside a stream
+ * capture. Every call on a device reuses the same array and leaves the
+ * previous call's data in it; each call writes every byte it later reads, so
+ * nothing needs to start at zero. Calls that overlap on the GPU (other threads,
+ * other contexts on the same device) race on the array and must be serialised
+ * by the caller; every return, on success or error, comes after the call's own
+ * GPU work has finished.
  */
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+
+#include <atomic>
 
 #include "scft_internal.h"
 
@@ -32,7 +39,9 @@
 
 static __device__ __align__(256) unsigned char g_scratch[SCFT_STATIC_SCRATCH_BYTES];
 
-static void *g_scratch_addr[SCFT_STATIC_MAX_DEVICES];
+/* per device: the array's device address, looked up once (atomic: first calls
+ * from several threads may race to store the same value) */
+static std::atomic<void *> g_scratch_addr[SCFT_STATIC_MAX_DEVICES];
 
 static size_t up256(size_t b) { return (b + 255) / 256 * 256; }
 
@@ -68,10 +77,10 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
         return SCFT_ERR_PARAM;
     }
     cudaError_t e = cudaSetDevice(dev);
-    if (e == cudaSuccess && !g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e == cudaSuccess) g_scratch_addr[dev] = p;
+    void *addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (e == cudaSuccess && !addr) {
+        e = cudaGetSymbolAddress(&addr, g_scratch);
+        if (e == cudaSuccess) g_scratch_addr[dev].store(addr, std::memory_order_release);
     }
     if (e != cudaSuccess) {
         char msg[256];
@@ -79,7 +88,18 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
         scft_set_error(msg);
         return SCFT_ERR_CUDA;
     }
-    unsigned char *base = static_cast<unsigned char *>(g_scratch_addr[dev]);
+    /* from here on work is queued on the stream: every return waits for it, so
+     * no error path leaves a copy or kernel writing the shared array */
+    auto fail = [&](cudaError_t err, int rc) {
+        cudaStreamSynchronize(st);
+        if (err != cudaSuccess) {
+            char msg[256];
+            snprintf(msg, sizeof(msg), "scft_propagate_static: %s", cudaGetErrorString(err));
+            scft_set_error(msg);
+        }
+        return rc;
+    };
+    unsigned char *base = static_cast<unsigned char *>(addr);
     ChainDesc *desc = reinterpret_cast<ChainDesc *>(base + o_desc);
     double *qd = reinterpret_cast<double *>(base + o_qd);
     void *q = base + o_q;
@@ -101,23 +121,13 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
     if (e == cudaSuccess) e = cudaMemcpyAsync(qd, q0, sizeof(double) * m, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = scft_boltz_one(prec, wd, bz, ds, m, st);
     if (e == cudaSuccess) e = scft_convert(prec, qd, q, m, 1, st);
-    if (e != cudaSuccess) {
-        char msg[256];
-        snprintf(msg, sizeof(msg), "scft_propagate_static: %s", cudaGetErrorString(e));
-        scft_set_error(msg);
-        return SCFT_ERR_CUDA;
-    }
+    if (e != cudaSuccess) return fail(e, SCFT_ERR_CUDA);
     int rc = scft_ctx_run_chain(ctx, desc, steps + 1);
-    if (rc != SCFT_OK) return rc;
+    if (rc != SCFT_OK) return fail(cudaSuccess, rc);
     e = scft_convert(prec, static_cast<const double *>(q), qd, (long)(sm * slices), 0, st);
     for (size_t s = 0; s < slices && e == cudaSuccess; ++s)
         e = cudaMemcpyAsync(q_out + s * m, qd + s * sm, sizeof(double) * m, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-        char msg[256];
-        snprintf(msg, sizeof(msg), "scft_propagate_static: %s", cudaGetErrorString(e));
-        scft_set_error(msg);
-        return SCFT_ERR_CUDA;
-    }
+    if (e != cudaSuccess) return fail(e, SCFT_ERR_CUDA);
     return SCFT_OK;
 }

@@ -101,22 +101,26 @@ def run_directory(path, precision: str = "fp64", use_graph: bool = False) -> Run
     wMask.dat (MASK 1). Writes the same output files there."""
     path = Path(path)
     surface = Surface.from_parameters_h((path / "parameters.h").read_text())
-    d = S.derive(surface)
-    if d.status != 0:
-        S.write_volume_error(path, d.c.volume_sum)
-        raise SystemExit(0)
-    counter = S.read_counter(path)
-    mask3 = S.read_mask(path, d) if surface.MASK else None
-    if counter > 0:
-        w14 = S.read_restart_fields(path, d)
-        seed = S.read_restart_random(path)
-    else:
-        w14 = None
-        ns = time.time_ns() % 1_000_000_000
-        seed = (ns & 0xFFFF, (ns + 1) & 0xFFFF, (ns + 2) & 0xFFFF)
-    S.write_run_params(path, surface, d, counter)
-    r = Run(surface, w14, counter, seed, mask3, precision=precision, outdir=path, use_graph=use_graph)
-    r.run_to_end()
+    S.set_file_names(surface)
+    try:
+        d = S.derive(surface)
+        if d.status != 0:
+            S.write_volume_error(path, d.c.volume_sum)
+            raise SystemExit(0)
+        counter = S.read_counter(path)
+        mask3 = S.read_mask(path, d) if surface.MASK else None
+        if counter > 0:
+            w14 = S.read_restart_fields(path, d)
+            seed = S.read_restart_random(path)
+        else:
+            w14 = None
+            ns = time.time_ns() % 1_000_000_000
+            seed = (ns & 0xFFFF, (ns + 1) & 0xFFFF, (ns + 2) & 0xFFFF)
+        S.write_run_params(path, surface, d, counter)
+        r = Run(surface, w14, counter, seed, mask3, precision=precision, outdir=path, use_graph=use_graph)
+        r.run_to_end()
+    finally:
+        S.set_file_names(None)
     return r
 
 

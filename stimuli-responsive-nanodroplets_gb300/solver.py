@@ -311,6 +311,28 @@ def write_run_params(path, s: Surface, d: Derived, it: int):
     L.check(L.lib().scft_write_run_params(_dir(path), C.byref(cs), C.byref(d.c), int(it)), "scft_write_run_params")
 
 
+#: parameters.h file-name macro -> scft_file_names field
+_NAME_FIELD = {"COUNTER": "counter", "DENSITY": "density", "DEVIATIONS": "deviations", "ENERGY": "energy",
+               "RESTART_FIELDS": "restart_fields", "RESTART_RANDOM": "restart_random", "RUN_PARAMS": "run_params",
+               "W_MASK": "w_mask", "FREE_ENERGY": "free_energy"}
+
+
+def set_file_names(s: Optional[Surface]):
+    """Name the text files after the surface's file-name macros (SCFT.c opens
+    them through COUNTER ... FREE_ENERGY, parameters.h:181-190); None restores
+    the reference's names. Process-wide, like the reference's compiled-in names."""
+    if s is None:
+        L.check(L.lib().scft_set_file_names(None), "scft_set_file_names")
+        return
+    n = L.CFileNames()
+    for macro, field in _NAME_FIELD.items():
+        v = s.file_name(macro).encode()
+        if not v or len(v) >= L.NAME_MAX:
+            raise ValueError(f"file name for {macro}: {v!r}")
+        setattr(n, field, v)
+    L.check(L.lib().scft_set_file_names(C.byref(n)), "scft_set_file_names")
+
+
 def write_volume_error(path, volume_sum: float):
     L.check(L.lib().scft_write_volume_error(_dir(path), float(volume_sum)), "scft_write_volume_error")
 

@@ -40,6 +40,14 @@ INT_MACROS = ["ITER", "D_WRT", "RELAXATION", "D_WRT_ENERGIES", "MASK", "ENABLE_S
               "SEED_AREA_DELTA", "NS"]
 
 
+#: the file-name macros of parameters.h (parameters.h:181-190) and the reference's names
+FILE_MACROS: Dict[str, str] = {
+    "COUNTER": "counter.dat", "DENSITY": "densities_dbk_", "DEVIATIONS": "deviations.dat",
+    "ENERGY": "energies.dat", "RESTART_FIELDS": "restart_fields.dat", "RESTART_RANDOM": "restart_random.dat",
+    "RUN_PARAMS": "run.txt", "W_MASK": "wMask.dat", "FREE_ENERGY": "free_energy.dat",
+}
+
+
 def _chi_names() -> List[str]:
     names = []
     for f in range(10):
@@ -75,6 +83,11 @@ class Surface:
     LEN_HOMO: List[float] = dataclasses.field(default_factory=lambda: [1.0] * 10)
     VOL_S: List[float] = dataclasses.field(default_factory=lambda: [0.0, 0.0, 0.0])
     LEN_S: List[float] = dataclasses.field(default_factory=lambda: [0.1, 0.1, 0.1])
+    #: file names (macro -> name); missing macros keep the reference's names
+    FILES: Dict[str, str] = dataclasses.field(default_factory=dict)
+
+    def file_name(self, macro: str) -> str:
+        return (getattr(self, "FILES", None) or {}).get(macro, FILE_MACROS[macro])
 
     # ------------------------------------------------------------------ chi
     def chi_n(self, f: int, g: int) -> float:
@@ -136,11 +149,9 @@ class Surface:
             L.append(f"#define G{gi}   G1 / 6.0")
         L += ["", "#define DX  (LX/NX)", "#define DY  (LY/NY)", "#define DZ  (LZ/NZ)", "",
               "#define ALPHAX  (DS/(DX*DX))", "#define ALPHAY  (DS/(DY*DY))", "#define ALPHAZ  (DS/(DZ*DZ))", "",
-              '#define COUNTER "counter.dat"', '#define DENSITY "densities_dbk_"',
-              '#define DEVIATIONS  "deviations.dat"', '#define ENERGY  "energies.dat"',
-              '#define RESTART_FIELDS  "restart_fields.dat"', '#define RESTART_RANDOM  "restart_random.dat"',
-              '#define RUN_PARAMS  "run.txt"', '#define W_MASK  "wMask.dat"', '#define FREE_ENERGY "free_energy.dat"',
-              ""]
+              "// File names"]
+        L += [f'#define {m} "{self.file_name(m)}"' for m in FILE_MACROS]
+        L.append("")
         return "\n".join(L)
 
     # -------------------------------------------------------------- parsing
@@ -148,17 +159,23 @@ class Surface:
     def from_parameters_h(cls, text: str) -> "Surface":
         """Parse the numeric macros of a parameters.h (comments allowed)."""
         vals: Dict[str, float] = {}
+        files: Dict[str, str] = {}
         for line in text.splitlines():
             line = line.split("//", 1)[0]
             m = re.match(r"\s*#define\s+([A-Z0-9_]+)\s+(.+?)\s*$", line)
             if not m:
                 continue
             name, expr = m.group(1), m.group(2)
+            q = re.fullmatch(r'"([^"]*)"', expr)
+            if q and name in FILE_MACROS:
+                files[name] = q.group(1)
+                continue
             try:
                 vals[name] = float(expr)
             except ValueError:
-                continue  # derived macros (DS, G2.., DX.., file names)
+                continue  # derived macros (DS, G2.., DX..)
         s = cls()
+        s.FILES = {k: v for k, v in files.items() if v != FILE_MACROS[k]}
         for name in ["LX", "LY", "LZ", "DT_NOISE", "DR_TARGET", "G1"]:
             if name in vals:
                 setattr(s, name, vals[name])
@@ -186,7 +203,8 @@ class Surface:
         return dataclasses.replace(self, chi=dict(self.chi), F_INPUT_DBK=list(self.F_INPUT_DBK),
                                    LEN_DBK=list(self.LEN_DBK), VOL_DBK=list(self.VOL_DBK),
                                    VOL_HOMO=list(self.VOL_HOMO), LEN_HOMO=list(self.LEN_HOMO),
-                                   VOL_S=list(self.VOL_S), LEN_S=list(self.LEN_S))
+                                   VOL_S=list(self.VOL_S), LEN_S=list(self.LEN_S),
+                                   FILES=dict(getattr(self, "FILES", None) or {}))
 
     def grid(self):
         """(NX, NY, NZ) by the reference's rounding rule (SCFT.c:103-105)."""

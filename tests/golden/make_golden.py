@@ -1,9 +1,10 @@
 """Generate the golden fixtures in tests/golden/ from the reference solver itself.
 
-Run in a checkout that has the reference source tree (default /root/reference,
-override with SCFT_REFERENCE_DIR):
+Run with SCFT_REFERENCE_DIR naming the reference source tree (the directory
+holding SCFT.c); the script stops with an error when it is unset:
 
-    python tests/golden/make_golden.py
+    SCFT_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py            # every fixture
+    SCFT_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py textnames  # renamed files only
 
 For every case it writes a parameters.h (stimuli-responsive-nanodroplets_gb300.surface)
 and the restart-path inputs (counter.dat, restart_fields.dat with %.17g,
@@ -54,17 +55,19 @@ def idx_order(nx, ny, nz):
 
 
 def write_inputs(d: Path, s, w14: np.ndarray, counter: int, seed=(11, 22, 33), mask3=None):
+    """The restart-path inputs, under the surface's file names (parameters.h
+    COUNTER, RESTART_FIELDS, RESTART_RANDOM, W_MASK)."""
     nx, ny, nz = s.grid()
     order = idx_order(nx, ny, nz)
-    (d / "counter.dat").write_text(f"{counter}")
+    (d / s.file_name("COUNTER")).write_text(f"{counter}")
     rows = [" ".join(f"{w14[c, idx]:.17g}" for c in range(14)) + " \n" for idx in order]
-    (d / "restart_fields.dat").write_text("".join(rows))
-    (d / "restart_random.dat").write_text(f"{seed[0]} {seed[1]} {seed[2]}")
+    (d / s.file_name("RESTART_FIELDS")).write_text("".join(rows))
+    (d / s.file_name("RESTART_RANDOM")).write_text(f"{seed[0]} {seed[1]} {seed[2]}")
     if s.MASK:
         if mask3 is None:
             mask3 = srn.configs.substrate_mask(s)
         rows = [f"{mask3[0, idx]:.17g} {mask3[1, idx]:.17g} {mask3[2, idx]:.17g}\n" for idx in order]
-        (d / "wMask.dat").write_text("".join(rows))
+        (d / s.file_name("W_MASK")).write_text("".join(rows))
     return mask3
 
 
@@ -117,15 +120,32 @@ def collect(name, s, d: Path, w14, counter, seed, mask3):
     print(f"{name}: {len(fe)} iterations, snapshot at {last.name}")
 
 
-def save_text(name, d: Path):
+def save_text(name, d: Path, mask_name: str = "wMask.dat"):
     out = GOLD / f"text_{name}"
     if out.exists():
         shutil.rmtree(out)
     out.mkdir()
     for f in sorted(d.iterdir()):
-        if f.suffix in (".dat", ".txt", ".error") and f.name not in ("wMask.dat",):
+        if f.suffix in (".dat", ".txt", ".error") and f.name != mask_name:
             shutil.copy(f, out / f.name)
     print(f"text_{name}: {sorted(p.name for p in out.iterdir())}")
+
+
+#: every file-name macro of parameters.h moved off the reference's default
+RENAMED = {"COUNTER": "cnt.dat", "DENSITY": "snap_", "DEVIATIONS": "dev.dat", "ENERGY": "en.dat",
+           "RESTART_FIELDS": "rf.dat", "RESTART_RANDOM": "rr.dat", "RUN_PARAMS": "params.txt",
+           "W_MASK": "mask_in.dat", "FREE_ENERGY": "fe.dat"}
+
+
+def text_names():
+    """The thin-film text case with every file renamed through parameters.h."""
+    s = srn.configs.film2d(nx=8, nz=6, ns=16, iters=2)
+    s.D_WRT = 1
+    s.FILES = dict(RENAMED)
+    w = srn.configs.droplet_fields(s, seed=107, radius=0.5)
+    d, _ = run_case("textnames", s, w, mask3=srn.configs.substrate_mask(s), text=True)
+    np.savez_compressed(GOLD / "text_inputs_names.npz", surface=json.dumps(s.__dict__), w0=w)
+    save_text("textnames", d, mask_name=RENAMED["W_MASK"])
 
 
 # ----------------------------------------------------------------- cases
@@ -297,7 +317,11 @@ def kat_density(tag: str, s, ns: int, blocks, seed: int):
 
 def main():
     if not obuild.reference_available():
-        raise SystemExit(f"reference source not found at {obuild.REFERENCE_SRC}")
+        raise SystemExit("set SCFT_REFERENCE_DIR to the reference source tree (the directory holding SCFT.c)"
+                         if obuild.REFERENCE_DIR is None else f"reference source not found at {obuild.REFERENCE_SRC}")
+    if sys.argv[1:] == ["textnames"]:
+        text_names()
+        return
     if sys.argv[1:] and all(a in FULL_SERIES for a in sys.argv[1:]):
         # full-size series alone (the blend takes about six minutes of one core)
         for name in sys.argv[1:]:
@@ -328,6 +352,7 @@ def main():
     d2, _ = run_case("textfilm", s2, w2, mask3=srn.configs.substrate_mask(s2), text=True)
     np.savez_compressed(GOLD / "text_inputs_film.npz", surface=json.dumps(s2.__dict__), w0=w2)
     save_text("textfilm", d2)
+    text_names()
     # volume check failure
     s3 = srn.configs.bulk2d(nx=8, nz=8, iters=1)
     s3.VOL_DBK = [0.9, 0.0, 0.0, 0.0]

@@ -64,5 +64,7 @@ def test_reference_arm_line(tmp_path):
     assert line["value"] > 0 and line["unit"] == "instance-iterations/s" and line["higher_is_better"] is True
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
     assert line["cpu_baseline"]["value"] == line["value"]
+    # the line states the steps it timed
+    assert line["steps"] == 1 and line["warmup"] == 0
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

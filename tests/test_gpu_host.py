@@ -21,9 +21,9 @@ def write_inputs(srn, d, S, w14, path, mask3):
             for i in range(nx):
                 idx = k + nz * (j + ny * i)
                 rows.append(" ".join(f"{w14[c, idx]:.17g}" for c in range(14)) + " \n")
-    (path / "restart_fields.dat").write_text("".join(rows))
-    (path / "counter.dat").write_text("1")
-    (path / "restart_random.dat").write_text("11 22 33")
+    (path / S.file_name("RESTART_FIELDS")).write_text("".join(rows))
+    (path / S.file_name("COUNTER")).write_text("1")
+    (path / S.file_name("RESTART_RANDOM")).write_text("11 22 33")
     if mask3 is not None:
         mrows = []
         for k in range(nz):
@@ -31,11 +31,14 @@ def write_inputs(srn, d, S, w14, path, mask3):
                 for i in range(nx):
                     idx = k + nz * (j + ny * i)
                     mrows.append(f"{mask3[0, idx]:.17g} {mask3[1, idx]:.17g} {mask3[2, idx]:.17g}\n")
-        (path / "wMask.dat").write_text("".join(mrows))
+        (path / S.file_name("W_MASK")).write_text("".join(mrows))
 
 
-@pytest.mark.parametrize("name,inputs,mask", [("textcase", "text_inputs", False), ("textfilm", "text_inputs_film", True)])
+@pytest.mark.parametrize("name,inputs,mask", [("textcase", "text_inputs", False), ("textfilm", "text_inputs_film", True),
+                                               ("textnames", "text_inputs_names", True)])
 def test_c_host_writes_reference_files(name, inputs, mask, srn, tmp_path):
+    """textnames renames every file through parameters.h's file-name macros:
+    the host reads and writes the renamed files, as SCFT.c did."""
     build = importlib.import_module("stimuli-responsive-nanodroplets_gb300.build")
     gi = dict(np.load(GOLD / f"{inputs}.npz"))
     S = surface_from_json(srn, gi["surface"])
@@ -49,6 +52,8 @@ def test_c_host_writes_reference_files(name, inputs, mask, srn, tmp_path):
     ref_dir = GOLD / f"text_{name}"
     for f in sorted(os.listdir(ref_dir)):
         assert (tmp_path / f).read_bytes() == (ref_dir / f).read_bytes(), f
+    if name == "textnames":
+        assert not (tmp_path / "counter.dat").exists() and not (tmp_path / "free_energy.dat").exists()
 
 
 def test_c_host_volume_check(srn, tmp_path):

@@ -150,25 +150,32 @@ def _oracle_run_text(srn, oracle_mod, surface, w0, mask3):
     return o
 
 
-@pytest.mark.parametrize("name,inputs,mask", [("textcase", "text_inputs", False), ("textfilm", "text_inputs_film", True)])
+@pytest.mark.parametrize("name,inputs,mask", [("textcase", "text_inputs", False), ("textfilm", "text_inputs_film", True),
+                                               ("textnames", "text_inputs_names", True)])
 def test_writers_byte_exact(name, inputs, mask, srn, oracle_mod, tmp_path):
+    """The library's writers against SCFT.c's files; textnames renames every
+    file through the file-name macros of parameters.h."""
     gi = dict(np.load(GOLD / f"{inputs}.npz"))
     S = surface_from_json(srn, gi["surface"])
     d = srn.derive(S)
     m3 = srn.configs.substrate_mask(S) if mask else None
     o = _oracle_run_text(srn, oracle_mod, S, gi["w0"], m3)
     saved = (11, 22, 33)
-    for _ in range(int(S.ITER)):
-        r = o.iterate(1)[0]
-        it = int(r[0])
-        rec = srn.IterOut(it, r[1], r[2], r[3], r[4:21], r[21:38], 0)
-        if it % int(S.D_WRT_ENERGIES) == 0:
-            srn.write_energies(tmp_path, d, rec)
-        if it % int(S.D_WRT) == 0 or it == 1:
-            phi, _ = o.densities()
-            srn.write_snapshot(tmp_path, d, it, phi, o.get_fields(), saved)
-            saved = o.get_rng()
-    srn.write_run_params(tmp_path, S, d, 1)
+    srn.set_file_names(S)
+    try:
+        for _ in range(int(S.ITER)):
+            r = o.iterate(1)[0]
+            it = int(r[0])
+            rec = srn.IterOut(it, r[1], r[2], r[3], r[4:21], r[21:38], 0)
+            if it % int(S.D_WRT_ENERGIES) == 0:
+                srn.write_energies(tmp_path, d, rec)
+            if it % int(S.D_WRT) == 0 or it == 1:
+                phi, _ = o.densities()
+                srn.write_snapshot(tmp_path, d, it, phi, o.get_fields(), saved)
+                saved = o.get_rng()
+        srn.write_run_params(tmp_path, S, d, 1)
+    finally:
+        srn.set_file_names(None)
     ref_dir = GOLD / f"text_{name}"
     for f in sorted(os.listdir(ref_dir)):
         got = (tmp_path / f).read_bytes()
@@ -197,3 +204,27 @@ def test_readers_roundtrip(srn, tmp_path):
                 rows.append(f"{m[0, idx]} {m[1, idx]} {m[2, idx]}\n")
     (tmp_path / "wMask.dat").write_text("".join(rows))
     np.testing.assert_array_equal(srn.read_mask(tmp_path, d), m)
+
+
+def test_allocation_free_entry_point_names_no_allocator():
+    """scft_propagate_static's source calls no device or pinned allocator (its
+    working buffers are the file-scope array)."""
+    import re
+    src = (GOLD.parents[1] / "stimuli-responsive-nanodroplets_gb300" / "csrc" / "scft_noalloc.cu").read_text()
+    code = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    code = re.sub(r"//[^\n]*", "", code)
+    for name in ("cudaMalloc", "cudaFree", "cudaMallocAsync", "cudaFreeAsync", "cudaMallocHost", "cudaHostAlloc",
+                 "cudaMallocManaged", "malloc(", "new "):
+        assert name not in code, name
+
+
+def test_file_name_macros_round_trip(srn):
+    """parameters.h's file-name macros survive the header generator and parser;
+    a header with the reference's names keeps no overrides."""
+    s = srn.configs.film2d(nx=8, nz=6, ns=16, iters=1)
+    assert srn.Surface.from_parameters_h(s.to_parameters_h()).FILES == {}
+    s.FILES = {"COUNTER": "runs/cnt.dat", "DENSITY": "snap_", "W_MASK": "m.dat"}
+    back = srn.Surface.from_parameters_h(s.to_parameters_h())
+    assert back.FILES == s.FILES
+    assert back.file_name("ENERGY") == "energies.dat" and back.file_name("COUNTER") == "runs/cnt.dat"
+

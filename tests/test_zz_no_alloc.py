@@ -58,3 +58,27 @@ def test_static_rejects_oversized_requests(srn):
         rc = lib.scft_propagate_static(sv._h, _dp(q0), _dp(w), steps, _dp(out))
         assert rc == -1
         assert b"fixed" in lib.scft_last_error()
+
+
+def test_static_call_allocates_no_device_memory(srn):
+    """The defining property: once the array's address is known (first call),
+    a call leaves the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    L = importlib.import_module("stimuli-responsive-nanodroplets_gb300._lib")
+    lib = L.lib()
+    g = load_golden("kat_prop_dirichlet2d")
+    S = surface_from_json(srn, g["surface"])
+    steps = g["q"].shape[0] - 1
+    with srn.Solver(S, precision="fp32") as sv:
+        q0 = np.ascontiguousarray(g["q0"])
+        w = np.ascontiguousarray(g["w"])
+        out = np.empty((steps + 1, sv.M))
+        L.check(lib.scft_propagate_static(sv._h, _dp(q0), _dp(w), steps, _dp(out)), "scft_propagate_static")
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for _ in range(3):
+            L.check(lib.scft_propagate_static(sv._h, _dp(q0), _dp(w), steps, _dp(out)), "scft_propagate_static")
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+    assert abs(free1 - free0) <= (2 << 20)
+
