@@ -140,7 +140,10 @@ int scft_set_iteration(scft_ctx *ctx, int instance, unsigned long iter);
  * runs ITER iterations; SCFT.c:1088): once an iteration ends with
  * RMS(phi_tot - 1) < rms_tol the instance is frozen. Later iterations of the
  * context skip all of its work (contour steps, densities, update, noise draws),
- * and its records repeat the converging iteration with converged = 1.
+ * and its records repeat the converging iteration with converged = 1. With a
+ * stop criterion an instance whose Q, free energy or RMS turns non-finite is
+ * frozen the same way (its records repeat status SCFT_ERR_NONFINITE) until
+ * scft_set_iteration re-arms it, which also clears the status.
  * rms_tol = 0 (the default) keeps the fixed-ITER semantics. */
 int scft_set_stop(scft_ctx *ctx, int instance, double rms_tol);
 /* Freeze an instance now (an idle slot): later iterations skip it until
@@ -182,7 +185,10 @@ int scft_iterate(scft_ctx *ctx, int n, const double *noise, scft_iter_out *out);
  * their own streams) busy at once: _async enqueues n <= SCFT_HIST_CAP
  * iterations without waiting (no host noise: SCFT_NOISE_DRAND48 or
  * MF*DT_NOISE == 0 throughout); _wait blocks until they finish and copies the
- * n * n_instances records to out (may be NULL). */
+ * n * n_instances records to out (may be NULL). When an instance's records
+ * carry SCFT_ERR_NONFINITE, _wait (like scft_iterate) still fills out with
+ * every instance's records and then returns SCFT_ERR_NONFINITE: the caller
+ * tells the failed instances from the others by their records' status. */
 #define SCFT_HIST_CAP 256
 int scft_iterate_async(scft_ctx *ctx, int n);
 int scft_iterate_wait(scft_ctx *ctx, scft_iter_out *out);
@@ -292,6 +298,11 @@ int scft_enable_timing(scft_ctx *ctx, int on);
 int scft_get_timing(const scft_ctx *ctx, scft_timing *t);
 
 const char *scft_last_error(void);
+
+/* Free and total device memory of a GPU (for admission by memory budget in
+ * the serving form; no counterpart in the reference). SCFT_ERR_NODEV without
+ * a usable device. */
+int scft_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
 
 /* ---------------------------------------------------------- host side */
 /* Fill noise for one iteration of one instance with the reference's draws:

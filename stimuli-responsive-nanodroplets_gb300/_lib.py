@@ -18,6 +18,7 @@ NF = 13
 NSP = 17
 
 SCFT_OK = 0
+ERR_NONFINITE = -4
 ERRORS = {
     -1: "SCFT_ERR_PARAM", -2: "SCFT_ERR_CUDA", -3: "SCFT_ERR_OOM", -4: "SCFT_ERR_NONFINITE",
     -5: "SCFT_ERR_VOLUME", -6: "SCFT_ERR_STATE", -7: "SCFT_ERR_IO", -8: "SCFT_ERR_NODEV",
@@ -174,6 +175,7 @@ def lib() -> C.CDLL:
         "scft_enable_timing": (I, [VP, I]),
         "scft_get_timing": (I, [VP, P(CTiming)]),
         "scft_last_error": (C.c_char_p, []),
+        "scft_device_memory": (I, [I, P(C.c_size_t), P(C.c_size_t)]),
         "scft_noise_fill": (I, [us3, P(CDerived), dp]),
         "scft_read_counter": (I, [C.c_char_p, P(UL)]),
         "scft_read_restart_fields": (I, [C.c_char_p, P(CDerived), dp]),

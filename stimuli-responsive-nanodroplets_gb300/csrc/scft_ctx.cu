@@ -39,6 +39,26 @@ static void set_err(const char *fmt, ...)
 
 extern "C" const char *scft_last_error(void) { return g_err; }
 
+extern "C" int scft_device_memory(int device, size_t *free_bytes, size_t *total_bytes)
+{
+    if (!free_bytes || !total_bytes) return SCFT_ERR_PARAM;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return SCFT_ERR_NODEV;
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMemGetInfo(free_bytes, total_bytes);
+    cudaSetDevice(cur);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return SCFT_ERR_CUDA;
+    }
+    return SCFT_OK;
+}
+
 #define CK(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
@@ -1190,6 +1210,8 @@ extern "C" int scft_set_iteration(scft_ctx *c, int b, unsigned long it)
     static const int zero = 0;
     CK(cudaMemcpyAsync(&c->state[b].iter, &c->iter[b], sizeof(unsigned long), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(&c->state[b].done, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    /* a re-armed instance starts without the error status of its last run */
+    CK(cudaMemcpyAsync(&c->state[b].status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SCFT_OK;
 }

@@ -538,6 +538,11 @@ __global__ void k_finalize(PostArgs a, int nparts)
         st.done = 2; /* frozen from the next iteration on; this one still ends with the p shift */
         rec.converged = 1;
     }
+    /* with a stop criterion (batch and serving forms) a non-finite instance is
+     * frozen too: its records repeat the failing iteration and it costs nothing
+     * until its slot is re-armed; without one (the fixed-ITER drop-in) it keeps
+     * iterating as the reference does */
+    if (st.stop_rms > 0.0 && st.status != SCFT_OK) st.done = 2;
     a.last[b] = rec;
     if (slot >= 0 && slot < a.hist_cap) a.hist[slot * a.B + b] = rec;
 }

@@ -31,7 +31,7 @@ from typing import Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .solver import Solver
+from .solver import Solver, device_memory
 from .surface import Surface
 
 
@@ -121,7 +121,7 @@ class Pool:
     def collect(self, now_fn: Callable[[], float], max_iter: int, keep_fields: bool) -> List[Completion]:
         if not self.in_flight:
             return []
-        recs = self.sv.iterate_wait()
+        recs = self.sv.iterate_wait(allow_nonfinite=True)  # a failed slot ends its own request only
         now = now_fn()
         self.in_flight = 0
         done = []
@@ -141,16 +141,30 @@ class Pool:
         return done
 
 
-def slots_for_budget(template: Surface, precision: str, budget_bytes: int, max_slots: int = 512) -> int:
+class BudgetError(ValueError):
+    """The memory budget does not hold one slot of the class."""
+
+
+def slots_for_budget(template: Surface, precision: str, budget_bytes: int, max_slots: int = 512,
+                     device: int = 0, reserve_frac: float = 0.05) -> int:
     """Slots of one class that fit a device-memory budget (bytes per slot
-    measured on a two-slot context, so shared tables are not counted twice)."""
-    with Solver([template], precision=precision, noise="device") as one:
+    measured on a two-slot context, so shared tables are not counted twice).
+    The budget is capped by the device's free memory less reserve_frac of its
+    total; a budget that cannot hold one slot raises BudgetError instead of
+    over-committing the device."""
+    with Solver([template], precision=precision, noise="device", device=device) as one:
         b1 = one.device_bytes
-    with Solver([template, template], precision=precision, noise="device") as two:
+    with Solver([template, template], precision=precision, noise="device", device=device) as two:
         b2 = two.device_bytes
     per_slot = max(1, b2 - b1)
     fixed = max(0, b1 - per_slot)
-    return int(max(1, min(max_slots, (budget_bytes - fixed) // per_slot)))
+    free, total = device_memory(device)
+    usable = min(int(budget_bytes), free - int(reserve_frac * total))
+    n = (usable - fixed) // per_slot
+    if n < 1:
+        raise BudgetError(f"a budget of {budget_bytes} bytes ({usable} usable of {free} free) holds no slot of "
+                          f"{fixed + per_slot} bytes")
+    return int(min(max_slots, n))
 
 
 class Server:

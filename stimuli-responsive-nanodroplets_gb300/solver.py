@@ -208,11 +208,16 @@ class Solver:
             L.check(r, "scft_iterate_ready")
         return bool(r)
 
-    def iterate_wait(self) -> List[List[IterOut]]:
+    def iterate_wait(self, allow_nonfinite: bool = False) -> List[List[IterOut]]:
+        """Records of the enqueued iterations, [iteration][instance].
+        allow_nonfinite: an instance that turned non-finite does not raise;
+        its records carry status SCFT_ERR_NONFINITE and the others are intact."""
         n = getattr(self, "_pending", 0)
         outs = (L.CIterOut * max(1, n * self.B))()
-        L.check(L.lib().scft_iterate_wait(self._h, outs), "scft_iterate_wait")
+        rc = L.lib().scft_iterate_wait(self._h, outs)
         self._pending = 0
+        if not (allow_nonfinite and rc == L.ERR_NONFINITE):
+            L.check(rc, "scft_iterate_wait")
         return [[IterOut.from_c(outs[k * self.B + b]) for b in range(self.B)] for k in range(n)]
 
     def get_fields(self, instance: int = 0) -> np.ndarray:
@@ -309,6 +314,13 @@ def write_snapshot(path, d: Derived, it: int, phi13: np.ndarray, w14: np.ndarray
 def write_run_params(path, s: Surface, d: Derived, it: int):
     cs = L.CSurface.from_surface(s)
     L.check(L.lib().scft_write_run_params(_dir(path), C.byref(cs), C.byref(d.c), int(it)), "scft_write_run_params")
+
+
+def device_memory(device: int = 0):
+    """(free, total) bytes of a GPU's memory."""
+    f, t = C.c_size_t(0), C.c_size_t(0)
+    L.check(L.lib().scft_device_memory(int(device), C.byref(f), C.byref(t)), "scft_device_memory")
+    return int(f.value), int(t.value)
 
 
 #: parameters.h file-name macro -> scft_file_names field

@@ -12,12 +12,13 @@ srn = importlib.import_module("stimuli-responsive-nanodroplets_gb300")
 
 
 class FakeRec:
-    def __init__(self, it, conv, F):
-        self.iter, self.converged, self.free_energy, self.rms, self.status = it, conv, F, 0.0 if conv else 1.0, 0
+    def __init__(self, it, conv, F, status=0):
+        self.iter, self.converged, self.free_energy, self.rms, self.status = it, conv, F, 0.0 if conv else 1.0, status
 
 
 class FakeSolver:
-    """Slot b of request r converges after need[r] iterations."""
+    """Slot b of request r converges after need[r] iterations; a negative
+    need[r] fails (status SCFT_ERR_NONFINITE) after -need[r] iterations."""
 
     def __init__(self, slots, need):
         self.B, self.need, self.M = slots, need, 8
@@ -58,19 +59,25 @@ class FakeSolver:
     def iterate_ready(self):
         return True
 
-    def iterate_wait(self):
+    def iterate_wait(self, allow_nonfinite=False):
         n, self.pending = self.pending, 0
-        recs = []
+        recs, failed = [], False
         for _ in range(n):
             row = []
             for b in range(self.B):
+                need = self.need[self.req[b]] if self.req[b] is not None else 0
                 if not self.frozen[b]:
                     self.it[b] += 1
-                    if self.it[b] - 1 >= self.need[self.req[b]]:
+                    if self.it[b] - 1 >= abs(need):
                         self.frozen[b] = True
                         self.log.append((self.req[b], self.it[b] - 1))
-                row.append(FakeRec(self.it[b], self.frozen[b] and self.req[b] is not None, float(self.req[b] or 0)))
+                bad = self.frozen[b] and need < 0 and self.it[b] - 1 >= -need
+                failed |= bad
+                row.append(FakeRec(self.it[b], self.frozen[b] and self.req[b] is not None and not bad,
+                                   float(self.req[b] or 0), -4 if bad else 0))
             recs.append(row)
+        if failed and not allow_nonfinite:
+            raise RuntimeError("SCFT_ERR_NONFINITE")
         return recs
 
     def get_fields(self, b):
@@ -143,3 +150,25 @@ def test_plane_surfaces_share_shape_within_a_class():
     for kind in ("lamellar", "cylinder", "disordered"):
         w = cfg.seed_fields(a, kind, seed=1)
         assert w.shape == (14, 32 * 16) and np.isfinite(w).all()
+
+
+def test_failed_request_ends_alone_and_frees_its_slot():
+    """A request whose instance turns non-finite completes with that status at
+    the next chunk boundary; its slot takes the next request, and every other
+    request completes as it would without it."""
+    need = [40, -15, 30, -5, 25, 35]
+    fake = FakeSolver(2, need)
+    pool = serve.Pool("c", None, 2, "fp32", solver=fake)
+    server = serve.Server({("c", "fp32"): pool}, rms_tol=1e-6, max_iter=1000, chunk=10)
+    done = {c.rid: c for c in server.run(make_requests(need), realtime=False)}
+    assert sorted(done) == list(range(len(need)))
+    for rid, n in enumerate(need):
+        c = done[rid]
+        if n < 0:
+            assert c.status == -4 and not c.converged and c.iterations == -n
+        else:
+            assert c.status == 0 and c.converged and c.iterations == n
+    assert not pool.busy and sorted(pool.free) == [0, 1]
+    # the two slots served all six requests: failed slots were reused
+    assert len({r for r, _ in fake.log}) == len(need)
+
