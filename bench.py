@@ -277,45 +277,67 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
     return res
 
 
-def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, fp64_iters: int, device: int, sync):
-    """The 2D droplet sweep (n x n chi points, uneven grids and NS) run to
-    RMS < rms_tol in the precision form: converged solves/hour. The plain FP64
-    form runs the same batch for fp64_iters iterations; its solves/hour is its
-    instance-iteration rate over the iterations the precision form needed per
-    solve (same start, same stop rule)."""
-    sw = importlib.import_module(f"{PKG}.sweep")
-    surfaces = srn.configs.sweep_surfaces(n, seed=3, sizes=sw.SWEEP_SIZES, ns_range=(64, 128))
-    inputs = sw.sweep_inputs(surfaces)
-    sync()
-    with sw.make_batch(surfaces, inputs, "fp32", rms_tol) as b:
+def _sweep_form(sw, surfaces, inputs, precision: str, rms_tol: float, max_iter: int, sync):
+    """One form of the droplet sweep run to the end (every instance converged
+    or at max_iter), timed from the batch's first iteration to its last."""
+    with sw.make_batch(surfaces, inputs, precision, rms_tol) as b:
+        sync()
         t0 = time.perf_counter()
         res = b.run(max_iter, chunk=200)
         sync()
-        wall32 = time.perf_counter() - t0
+        wall = time.perf_counter() - t0
         groups = b.groups
     its = np.array([r.iterations for r in res])
     conv = int(sum(r.converged for r in res))
-    out = {"instances": len(res), "groups": groups, "rms_tol": rms_tol, "max_iter": max_iter,
-           "fp32": {"converged": conv, "wall_s": wall32, "solves_per_hour": conv * 3600.0 / wall32,
-                    "iterations_median": float(np.median(its)), "iterations_max": int(its.max()),
-                    "instance_iterations_per_s": float(its.sum()) / wall32}}
-    if fp64_iters > 0:
-        with sw.make_batch(surfaces, inputs, "fp64", rms_tol) as b:
-            b.run(2, chunk=2)  # graph capture and first touch outside the timed region
-            sync()
-            t0 = time.perf_counter()
-            r64 = b.run(fp64_iters, chunk=min(fp64_iters, 200))
-            sync()
-            wall64 = time.perf_counter() - t0
-        done64 = sum(r.iterations for r in r64)
-        rate64 = done64 / wall64
-        per_solve = float(its.mean())
-        out["fp64_plain"] = {"instance_iterations_per_s": rate64, "iterations_timed": fp64_iters,
-                             "solves_per_hour": rate64 * 3600.0 / per_solve,
-                             "method": "rate over the first iterations x mean iterations per solve of the "
-                                       "precision form"}
-        out["solves_per_hour_ratio_fp32_over_fp64"] = out["fp32"]["solves_per_hour"] / out["fp64_plain"][
-            "solves_per_hour"]
+    by_shape = {}
+    for s, r in zip(surfaces, res):
+        nx, _, nz = s.grid()
+        d = by_shape.setdefault(f"{nx}x{nz}", {"instances": 0, "converged": 0, "final_rms": []})
+        d["instances"] += 1
+        d["converged"] += int(r.converged)
+        d["final_rms"].append(float(r.rms))
+    for d in by_shape.values():
+        v = np.array(d.pop("final_rms"))
+        d["final_rms_median"] = float(np.median(v))
+        d["final_rms_min"] = float(v.min())
+        d["final_rms_max"] = float(v.max())
+    return {"instances": len(res), "groups": groups, "converged": conv, "wall_s": wall,
+            "solves_per_hour": conv * 3600.0 / wall, "iterations_median": float(np.median(its)),
+            "iterations_max": int(its.max()), "instance_iterations_per_s": float(its.sum()) / wall,
+            "nonfinite": int(sum(r.status != 0 for r in res)), "by_shape": by_shape,
+            "final_rms": [float(r.rms) for r in res]}
+
+
+def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, device: int, sync,
+                  keep_points: bool = False):
+    """The 2D droplet sweep (n x n chi points, uneven grids and NS, seeded
+    droplet starts) run to RMS < rms_tol or max_iter, every form timed to the
+    end: converged solves/hour = converged instances / wall time.
+    fp32: the precision form on all n x n points. subset: every k-th point
+    (k = n*n / subset) in both forms, the plain FP64 form and the precision
+    form on the same instances, the same start and the same stop rule; their
+    ratio is read against the >= 5x target."""
+    sw = importlib.import_module(f"{PKG}.sweep")
+    surfaces = srn.configs.sweep_surfaces(n, seed=3, sizes=sw.SWEEP_SIZES, ns_range=(64, 128))
+    inputs = sw.sweep_inputs(surfaces)
+    full = _sweep_form(sw, surfaces, inputs, "fp32", rms_tol, max_iter, sync)
+    if not keep_points:
+        full.pop("final_rms")
+    out = {"rms_tol": rms_tol, "max_iter": max_iter, "fp32": full}
+    if subset > 0:
+        step = max(1, len(surfaces) // subset)
+        idx = list(range(0, len(surfaces), step))[:subset]
+        ss = [surfaces[i] for i in idx]
+        si = [inputs[i] for i in idx]
+        f32 = _sweep_form(sw, ss, si, "fp32", rms_tol, max_iter, sync)
+        f64 = _sweep_form(sw, ss, si, "fp64", rms_tol, max_iter, sync)
+        if not keep_points:
+            for f in (f32, f64):
+                f.pop("final_rms")
+        out["subset"] = {"points": idx, "fp32": f32, "fp64_plain": f64,
+                         "solves_per_hour_ratio_fp32_over_fp64": f32["solves_per_hour"] / f64["solves_per_hour"]
+                         if f64["solves_per_hour"] > 0 else None,
+                         "basis": "converged instances / wall time to the end, both forms on the same instances"}
     return out
 
 
@@ -574,11 +596,13 @@ def main():
     ap.add_argument("--sweep-n", type=int, default=16, help="n x n chi points of the droplet sweep (0: skip)")
     ap.add_argument("--sweep-tol", type=float, default=1e-4)
     ap.add_argument("--sweep-max-iter", type=int, default=5000)
-    ap.add_argument("--sweep-fp64-iters", type=int, default=20)
+    ap.add_argument("--sweep-subset", type=int, default=32,
+                    help="points of the sweep run in both forms to the end (0: precision form only)")
+    ap.add_argument("--sweep-points", action="store_true", help="keep every point's final RMS in the sweep record")
     ap.add_argument("--serve-requests", type=int, default=40, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=4.0, help="mean arrivals per second")
-    ap.add_argument("--serve-tol", type=float, default=1e-3)
-    ap.add_argument("--serve-max-iter", type=int, default=3000)
+    ap.add_argument("--serve-tol", type=float, default=1e-4)
+    ap.add_argument("--serve-max-iter", type=int, default=4000)
     ap.add_argument("--serve-winners", type=int, default=4,
                     help="points of the FP32-vs-FP64 lowest-F winner check after serving (0: skip)")
     ap.add_argument("--profile-case", action="store_true",
@@ -659,8 +683,8 @@ def main():
     if world > 1:
         args.sweep_n = args.serve_requests = 0
     if args.sweep_n > 0:
-        line["sweep"] = measure_sweep(srn, args.sweep_n, args.sweep_tol, args.sweep_max_iter, args.sweep_fp64_iters,
-                                      local, sync)
+        line["sweep"] = measure_sweep(srn, args.sweep_n, args.sweep_tol, args.sweep_max_iter, args.sweep_subset,
+                                      local, sync, keep_points=args.sweep_points)
     if args.serve_requests > 0:
         line["serving"] = measure_serving(srn, args.serve_requests, args.serve_rate, args.serve_tol,
                                           args.serve_max_iter, local, args.serve_winners)
