@@ -200,6 +200,7 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
         "algorithmic_bytes_per_step": bytes_iter * B,
         "contour_steps_per_instance_iteration": steps_iter,
         "device_bytes": sv.device_bytes,
+        "threads_per_line": int(t["threads_per_line"]),
         "kernel": {1: f"k_chain2d<float,{sv.grid[0]},{sv.grid[2]}> (persistent fused contour loop)",
                    2: "k_chain3d (64^3 contour loop, one 8-CTA cluster per chain)"}.get(
                        t["fused_chain"], "k_pass_fft + k_pass_dense (per-axis passes)"),
@@ -338,6 +339,21 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
                          "solves_per_hour_ratio_fp32_over_fp64": f32["solves_per_hour"] / f64["solves_per_hour"]
                          if f64["solves_per_hour"] > 0 else None,
                          "basis": "converged instances / wall time to the end, both forms on the same instances"}
+        if rms_tol < sw.SWITCH_RMS:
+            # below the FP32 floor: the precision form hands over to FP64 at SWITCH_RMS
+            sync()
+            res, wall, wall32 = sw.run_finished(ss, si, rms_tol, max_iter)
+            sync()
+            conv = int(sum(r.converged for r in res))
+            fin = {"switch_rms": sw.SWITCH_RMS, "converged": conv, "wall_s": wall, "fp32_phase_s": wall32,
+                   "solves_per_hour": conv * 3600.0 / wall,
+                   "iterations_median": float(np.median([r.iterations for r in res])),
+                   "fp32_iterations_median": float(np.median([r.iterations_fp32 for r in res]))}
+            if keep_points:
+                fin["final_rms"] = [float(r.rms) for r in res]
+            out["subset"]["fp32_fp64_finish"] = fin
+            out["subset"]["solves_per_hour_ratio_finish_over_fp64"] = (
+                fin["solves_per_hour"] / f64["solves_per_hour"] if f64["solves_per_hour"] > 0 else None)
     return out
 
 
@@ -596,7 +612,7 @@ def main():
     ap.add_argument("--sweep-n", type=int, default=16, help="n x n chi points of the droplet sweep (0: skip)")
     ap.add_argument("--sweep-tol", type=float, default=1e-4)
     ap.add_argument("--sweep-max-iter", type=int, default=5000)
-    ap.add_argument("--sweep-subset", type=int, default=32,
+    ap.add_argument("--sweep-subset", type=int, default=16,
                     help="points of the sweep run in both forms to the end (0: precision form only)")
     ap.add_argument("--sweep-points", action="store_true", help="keep every point's final RMS in the sweep record")
     ap.add_argument("--serve-requests", type=int, default=40, help="requests of the serving stream (0: skip)")
@@ -677,7 +693,8 @@ def main():
                        "prop_ms_per_step": f64["prop_ms_per_step"], "clocks": f64["clocks"]},
         "detail": {"fp32_prop_ms_per_step": f32["prop_ms_per_step"], "fp32_wall_ms_per_step": f32["wall_ms_per_step"],
                    "contour_steps_per_instance_iteration": f32["contour_steps_per_instance_iteration"],
-                   "device_bytes_fp32": f32["device_bytes"]},
+                   "device_bytes_fp32": f32["device_bytes"],
+                   "fp32_threads_per_line": f32["threads_per_line"]},
     }
     # the sweep and the serving stream are single-GPU measurements (replicas add nothing to them)
     if world > 1:

@@ -823,6 +823,68 @@ static int autotune_axes(scft_ctx *c)
     return rc;
 }
 
+/* The fused 2D contour loop's launch form: one or two threads per line (every
+ * value computed by the same arithmetic either way, so results are
+ * bit-identical). Both are timed on the context's own chains (one persistent
+ * launch of a whole iteration's contour steps, after a warm-up launch) and the
+ * faster is kept, cached per (shape, precision, chains, contour length). The
+ * launches run on whatever the chains' buffers hold at creation: the timing
+ * does not depend on the values, and every buffer is rewritten before use. */
+static int autotune_fused2d(scft_ctx *c)
+{
+    if (!c->fused2d || !scft_step2d_wide(c->opt.precision, c->nx, c->nz)) return SCFT_OK;
+    const int total = c->B * c->nchains;
+    char key[160];
+    snprintf(key, sizeof(key), "fused2d|%d|%d,%d|%d|%d", c->psize, c->nx, c->nz, total, c->maxlen);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            c->wide2d = it->second;
+            return SCFT_OK;
+        }
+    }
+    Step2DArgs a;
+    memset(&a, 0, sizeof(a));
+    a.chains = c->chains;
+    a.order = c->order;
+    a.state = nullptr; /* every chain runs */
+    a.s = 0;
+    a.s_end = c->maxlen - 1;
+    a.sstride = c->sm;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    int best = c->wide2d;
+    cudaError_t e = cudaSuccess;
+    for (int wide = 0; wide <= 1 && e == cudaSuccess; ++wide) {
+        e = scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, total, c->stream, 0, wide); /* warm-up */
+        if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r)
+            e = scft_launch_step2d(c->opt.precision, c->nx, c->nz, a, total, c->stream, 0, wide);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && ms < best_ms) {
+            best_ms = ms;
+            best = wide;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        set_err("autotune: %s", cudaGetErrorString(e));
+        return SCFT_ERR_CUDA;
+    }
+    scft_step2d_take_fault(); /* a tensor-core wait that gave up on the timing runs is not an iteration's */
+    c->wide2d = best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = best;
+    return SCFT_OK;
+}
+
 /* Instances of one context share the grid, the MASK setting and the active
  * field set (the noise layout); the species composition is compared after the
  * chains are built. */
@@ -1155,6 +1217,10 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
             scft_ctx_destroy(c);
             return rc;
         }
+    }
+    if (opt.autotune && c->fused2d && (rc = autotune_fused2d(c))) {
+        scft_ctx_destroy(c);
+        return rc;
     }
     c->iter.assign(B, 0);
     c->rng.assign(3 * B, 0);

@@ -84,6 +84,60 @@ def run_sweep(n: int = 16, precision: str = "fp32", rms_tol: float = 1e-6, max_i
     return SweepRun(res, wall, groups, precision)
 
 
+#: RMS at which the precision form hands an instance to the plain FP64 form
+#: (run_finished): a few times above the FP32 form's RMS floor, which is
+#: 3e-6 - 9e-6 on the sweep shapes (FP32 rounding of the propagators puts that
+#: much relative noise into phi_tot; measured over 12000 iterations)
+SWITCH_RMS = 2e-5
+
+
+@dataclass
+class FinishedResult:
+    iterations: int       # both phases
+    iterations_fp32: int
+    rms: float
+    free_energy: float
+    converged: bool       # RMS < rms_tol within max_iter iterations in all
+    status: int
+
+
+def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: int, switch_rms: float = SWITCH_RMS,
+                 chunk: int = 200, use_graph: bool = True):
+    """The precision form run to an RMS below its FP32 floor: every instance
+    iterates in FP32 until RMS < switch_rms, then continues from its fields in
+    the plain FP64 form until RMS < rms_tol; max_iter bounds the two phases
+    together. Returns (results, wall seconds, seconds of the FP32 phase). The
+    iteration is the reference's update in both phases; only the propagators'
+    precision changes at the hand-over."""
+    t0 = time.perf_counter()
+    with make_batch(surfaces, inputs, "fp32", switch_rms, use_graph) as b:
+        r32 = b.run(max_iter, chunk)
+        handoff = [i for i, r in enumerate(r32) if r.converged and r.status == 0]
+        fields = {i: b.get_fields(i) for i in handoff}
+    t1 = time.perf_counter()
+    out = [FinishedResult(r.iterations, r.iterations, r.rms, r.free_energy, False, r.status) for r in r32]
+    if handoff:
+        sub = [surfaces[i] for i in handoff]
+        left = max_iter - min(r32[i].iterations for i in handoff)
+        b64 = Batch(sub, precision="fp64", use_graph=use_graph, noise="device")
+        try:
+            for k, i in enumerate(handoff):
+                b64.set_fields(k, fields[i])
+                b64.set_masks(k, inputs[i][1])
+                b64.set_iteration(k, r32[i].iter)
+                b64.set_rng(k, (11 + i, 22, 33))
+                b64.set_stop(k, rms_tol)
+            r64 = b64.run(max(1, left), chunk)
+        finally:
+            b64.close()
+        for k, i in enumerate(handoff):
+            r = r64[k]
+            total = r32[i].iterations + r.iterations
+            out[i] = FinishedResult(total, r32[i].iterations, r.rms, r.free_energy,
+                                    bool(r.converged) and total <= max_iter, r.status)
+    return out, time.perf_counter() - t0, t1 - t0
+
+
 def summary(run: SweepRun) -> dict:
     it = np.array([r.iterations for r in run.results])
     return {"precision": run.precision, "instances": len(run.results), "converged": run.converged,

@@ -70,7 +70,9 @@ def test_two_threads_per_line_bit_identical(srn, nx, nz):
     m = srn.configs.substrate_mask(s)
 
     def run(B):
-        with srn.Solver([s] * B, precision="fp32") as sv:
+        # the heuristic form (autotune off): two threads per line exactly when
+        # the batch has at most one chain per SM
+        with srn.Solver([s] * B, precision="fp32", autotune=False) as sv:
             tpl = sv.timing()["threads_per_line"]
             for b in range(B):
                 sv.set_fields(w, b)

@@ -1,7 +1,12 @@
 """The 64^3 cluster-resident contour loop (FP32, MASK 0) against the FP64
-plain form and against the FP32 per-axis passes."""
+plain form, against the FP32 per-axis passes, and directly against the
+reference's own series of the four-diblock blend at 64^3."""
+import importlib
+
 import numpy as np
 import pytest
+
+from conftest import load_golden, surface_from_json
 
 pytestmark = pytest.mark.gpu
 
@@ -56,3 +61,25 @@ def test_fused3d_iterations_vs_fp64_and_batch(srn):
         o = solo.iterate(3)
         assert o[-1][0].free_energy == res["fp32"][0][-1][1].free_energy
         np.testing.assert_array_equal(solo.get_fields(), res["fp32"][1])
+
+
+def test_fused3d_against_reference_series(srn):
+    """The four-diblock blend of the third configuration (64^3, NS 128, 11
+    chains, noise from the drand48 replay) through the cluster kernel: it runs
+    the fused loop, and every iteration's free energy is within 3e-6 of the
+    reference's own (tests/golden/blend3d_full, SCFT.c on the same start)."""
+    g = load_golden("blend3d_full")
+    S = surface_from_json(srn, g["surface"])
+    w0 = srn.configs.uniform_fields(S.grid(), seed=1000, amp=0.1, fields=tuple(range(9)))
+    np.testing.assert_allclose(w0.sum(axis=1), g["w_sum"], rtol=0, atol=1e-9)
+    runner = importlib.import_module("stimuli-responsive-nanodroplets_gb300.runner")
+    r = runner.Run(S, w0, int(g["counter"]), tuple(int(x) for x in g["seed0"]), None, precision="fp32",
+                   noise="device")
+    r.solver.enable_timing(True)
+    r.run_to_end()
+    assert r.solver.timing()["fused_chain"] == 2
+    by_iter = {rec.iter: rec for rec in r.records}
+    for row in g["free_energy"]:
+        got = by_iter[int(row[0])].free_energy
+        assert abs(got - row[1]) <= 3e-6 * abs(row[1]), (row[0], got, row[1])
+

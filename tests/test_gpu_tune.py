@@ -1,6 +1,7 @@
-"""The pass-tile autotuner changes launch shapes only: results with tuned and
-heuristic tiles are bit-identical (3D periodic FFT passes, 2D Dirichlet dense
-passes in FP64, both precisions)."""
+"""The autotuner changes launch shapes only: results with tuned and heuristic
+tiles are bit-identical (3D periodic FFT passes, 2D Dirichlet dense passes in
+FP64, both precisions), and so are the fused 2D loop's tuned and heuristic
+launch forms."""
 import numpy as np
 import pytest
 
@@ -37,3 +38,30 @@ def test_autotune_invariant_film_passes(srn, precision):
     b = _run(srn, s, w, m, precision, False, kernel_path="passes")
     assert a[0] == b[0]
     np.testing.assert_array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("B", [2, 40])
+def test_autotune_invariant_fused_loop(srn, B):
+    """The fused FP32 2D loop (tensor-core z tail) with its launch form timed at
+    context creation against the heuristic form: the same records and fields,
+    bit for bit, for a batch below and one above one chain per SM."""
+    s = srn.configs.film2d(nx=192, nz=96, ns=40, iters=3)
+    w = srn.configs.droplet_fields(s, seed=5)
+    m = srn.configs.substrate_mask(s)
+
+    def run(tune):
+        with srn.Solver([s.copy() for _ in range(B)], precision="fp32", autotune=tune) as sv:
+            tpl = sv.timing()["threads_per_line"]
+            for b in range(B):
+                sv.set_fields(w, b)
+                sv.set_masks(m, b)
+                sv.set_iteration(1, b)
+            out = sv.iterate(3)
+            return tpl, [o[B - 1].free_energy for o in out], sv.get_fields(B - 1)
+
+    ta, fa, wa = run(True)
+    tb, fb, wb = run(False)
+    assert ta in (1, 2) and tb in (1, 2)
+    assert fa == fb
+    np.testing.assert_array_equal(wa, wb)
+

@@ -25,6 +25,24 @@ def test_small_sweep_runs_to_tolerance(srn):
     assert st["converged"] >= 1
 
 
+def test_fp32_with_fp64_finish_reaches_the_fp64_fixed_point(srn):
+    """Below the FP32 form's RMS floor the precision form hands each instance
+    over to the plain FP64 form: it converges to the tolerance, to the free
+    energy the plain FP64 form reaches on its own (1e-6 relative), having run
+    its first iterations in FP32."""
+    cfg = srn.configs
+    surfaces = cfg.sweep_surfaces(2, seed=1, sizes=((32, 16), (48, 16)), ns_range=(40, 60))
+    inputs = sweep.sweep_inputs(surfaces)
+    res, wall, wall32 = sweep.run_finished(surfaces, inputs, rms_tol=1e-5, max_iter=8000, switch_rms=1e-4)
+    with sweep.make_batch(surfaces, inputs, "fp64", 1e-5) as b:
+        ref = b.run(8000, chunk=200)
+    assert 0 < wall32 < wall
+    for r, f in zip(res, ref):
+        assert r.status == 0 and f.converged
+        assert r.converged and r.rms < 1e-5 and 0 < r.iterations_fp32 < r.iterations
+        assert abs(r.free_energy - f.free_energy) <= 1e-6 * abs(f.free_energy)
+
+
 def _film(cfg, p, chi_ab, chi_ac, prec_ns=40):
     return cfg.film_point(chi_ab, chi_ac, cfg.PLANES[p], nx=32, nz=16, ns=prec_ns)
 
