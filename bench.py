@@ -621,6 +621,7 @@ def main():
     ap.add_argument("--serve-max-iter", type=int, default=4000)
     ap.add_argument("--serve-winners", type=int, default=4,
                     help="points of the FP32-vs-FP64 lowest-F winner check after serving (0: skip)")
+    ap.add_argument("--profile-iters", type=int, default=1, help="iterations of --profile-case")
     ap.add_argument("--profile-case", action="store_true",
                     help="one iteration of one form only (for ncu captures); prints no bench line")
     args = ap.parse_args()
@@ -656,9 +657,10 @@ def main():
             if m is not None:
                 sv.set_masks(m, b)
             sv.set_iteration(start_iteration(s), b)
-        out = sv.iterate(1)
+        out = sv.iterate(args.profile_iters)
         torch.cuda.synchronize()
-        print(f"profile case: {len(surfaces)} instances, F[0] = {out[0][0].free_energy:.12f}")
+        print(f"profile case: {len(surfaces)} instances, {args.profile_iters} iteration(s), "
+              f"F[0] = {out[-1][0].free_energy:.12f}")
         sv.close()
         return
     f32 = measure_form(srn, surfaces, "fp32", args.steps, args.warmup, local, sync, args.e2e_steps, args.e2e_parts)
