@@ -314,8 +314,8 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
     """The 2D droplet sweep (n x n chi points, uneven grids and NS, seeded
     droplet starts) run to RMS < rms_tol or max_iter, every form timed to the
     end: converged solves/hour = converged instances / wall time.
-    fp32: the precision form on all n x n points. subset: every k-th point
-    (k = n*n / subset) in both forms, the plain FP64 form and the precision
+    fp32: the precision form on all n x n points. subset: points on a diagonal
+    walk of the chi grid in both forms, the plain FP64 form and the precision
     form on the same instances, the same start and the same stop rule; their
     ratio is read against the >= 5x target."""
     sw = importlib.import_module(f"{PKG}.sweep")
@@ -326,8 +326,9 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
         full.pop("final_rms")
     out = {"rms_tol": rms_tol, "max_iter": max_iter, "fp32": full}
     if subset > 0:
-        step = max(1, len(surfaces) // subset)
-        idx = list(range(0, len(surfaces), step))[:subset]
+        # spread over both chi axes: point j sits in row j*n/subset of the grid,
+        # column j mod n (a diagonal walk), so every chi_AB and chi_AC band is in
+        idx = sorted({(j * n // subset) * n + (j % n) for j in range(subset)} & set(range(len(surfaces))))
         ss = [surfaces[i] for i in idx]
         si = [inputs[i] for i in idx]
         f32 = _sweep_form(sw, ss, si, "fp32", rms_tol, max_iter, sync)
