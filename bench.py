@@ -228,7 +228,9 @@ def measure_form(srn, surfaces, precision: str, steps: int, warmup: int, device:
         parts = []
         for k in range(e2e_parts):
             lo, hi = int(bounds[k]), int(bounds[k + 1])
-            psv = srn.Solver(surfaces[lo:hi], precision=precision, device=device, noise="device")
+            # the parts run side by side: launch forms tuned on one part alone would not be the
+            # fastest with the other parts in flight, so they keep the heuristic forms
+            psv = srn.Solver(surfaces[lo:hi], precision=precision, device=device, noise="device", autotune=False)
             for j, b in enumerate(range(lo, hi)):
                 if init[b][1] is not None:
                     psv.set_masks(init[b][1], j)

@@ -108,9 +108,13 @@ typedef struct scft_options {
     int n_instances; /* instances in this context (batching form); 1 for a single solve */
     int kernel_path; /* 0: fused single-launch contour step where the shape has one, else per-axis
                         passes; 1: per-axis passes only */
-    int autotune;    /* 1 (default): time the per-axis pass tile candidates on the context's own
-                        chains at creation and keep the fastest (cached per shape and batch size);
-                        0: heuristic tiles. Every candidate gives bit-identical results. */
+    int autotune;    /* 1 (default): time the launch forms on the context's own chains at
+                        creation and keep the fastest (cached per shape and batch size): per-axis
+                        pass tiles, the fused 2D loop's one or two threads per line; 0: heuristics.
+                        Every candidate gives bit-identical results. The timing is taken with the
+                        context alone on the GPU: contexts whose iterations are kept in flight side
+                        by side (pipelined parts of one batch, serving pools) run better on the
+                        heuristic forms. */
     int reserved;
 } scft_options;
 

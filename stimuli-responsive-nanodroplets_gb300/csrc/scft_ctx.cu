@@ -774,8 +774,11 @@ static int autotune_axes(scft_ctx *c)
                 continue;
             }
         }
+        /* every divisor up to 64 (even ones for the FFT passes), not only powers of
+         * two: with few chains (a single solve) a tile that gives about one CTA per
+         * SM avoids a second, mostly empty wave */
         std::vector<int> cand;
-        for (int t = A.g.dirichlet ? 1 : 2; t <= 64; t *= 2)
+        for (int t = A.g.dirichlet ? 1 : 2; t <= 64; t += A.g.dirichlet ? 1 : 2)
             if (divisor % t == 0 && lines / t >= 1 && scft_pass_smem_bytes(A.g, t, A.h, c->psize) <= (size_t)optin)
                 cand.push_back(t);
         if (cand.size() > 1) {

@@ -80,8 +80,10 @@ class Pool:
                  solver=None, chunk: Optional[int] = None):
         self.cls, self.precision, self.slots = cls, precision, int(slots)
         self.chunk = chunk  # iterations per round (None: the server's)
+        # pools run side by side: launch forms tuned on one pool alone would not be the
+        # fastest with the others in flight, so pools keep the heuristic forms
         self.sv = solver if solver is not None else Solver([template] * self.slots, precision=precision,
-                                                            use_graph=use_graph, noise="device")
+                                                            use_graph=use_graph, noise="device", autotune=False)
         zero = np.zeros((14, self.sv.M))
         for b in range(self.slots):
             self.sv.set_fields(zero, b)
