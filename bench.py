@@ -343,12 +343,15 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
                          if f64["solves_per_hour"] > 0 else None,
                          "basis": "converged instances / wall time to the end, both forms on the same instances"}
         if rms_tol < sw.SWITCH_RMS:
-            # below the FP32 floor: the precision form hands over to FP64 at SWITCH_RMS
+            # below the FP32 floor: the precision form hands over to FP64 on its floor
             sync()
             res, wall, wall32 = sw.run_finished(ss, si, rms_tol, max_iter)
             sync()
             conv = int(sum(r.converged for r in res))
-            fin = {"switch_rms": sw.SWITCH_RMS, "converged": conv, "wall_s": wall, "fp32_phase_s": wall32,
+            fin = {"handover": f"RMS < {sw.SWITCH_RMS:g} and falling by less than {1 - sw.STALL_GAIN:g} over "
+                               f"{sw.STALL_ROUND} iterations, or RMS < {sw.FLOOR_RMS:g}; max_iter per instance "
+                               f"over both phases",
+                   "converged": conv, "wall_s": wall, "fp32_phase_s": wall32,
                    "solves_per_hour": conv * 3600.0 / wall,
                    "iterations_median": float(np.median([r.iterations for r in res])),
                    "fp32_iterations_median": float(np.median([r.iterations_fp32 for r in res]))}

@@ -84,11 +84,16 @@ def run_sweep(n: int = 16, precision: str = "fp32", rms_tol: float = 1e-6, max_i
     return SweepRun(res, wall, groups, precision)
 
 
-#: RMS at which the precision form hands an instance to the plain FP64 form
-#: (run_finished): a few times above the FP32 form's RMS floor, which is
-#: 3e-6 - 9e-6 on the sweep shapes (FP32 rounding of the propagators puts that
-#: much relative noise into phi_tot; measured over 12000 iterations)
+#: Hand-over of the precision form to the plain FP64 form (run_finished): an
+#: instance moves once its FP32 RMS is below SWITCH_RMS and has stopped falling
+#: (less than STALL_GAIN over STALL_ROUND iterations), i.e. once it sits on the
+#: FP32 form's RMS floor (3e-6 - 9e-6 on the sweep shapes: FP32 rounding of the
+#: propagators puts that much relative noise into phi_tot), or once it is below
+#: FLOOR_RMS, under which the FP32 form does not go.
 SWITCH_RMS = 2e-5
+FLOOR_RMS = 3e-6
+STALL_ROUND = 400
+STALL_GAIN = 0.8
 
 
 @dataclass
@@ -101,40 +106,77 @@ class FinishedResult:
     status: int
 
 
+def _freeze(b: Batch, i: int):
+    """An instance stops at the end of its next iteration (any RMS is below the tolerance)."""
+    b.set_stop(i, 1e300)
+
+
 def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: int, switch_rms: float = SWITCH_RMS,
-                 chunk: int = 200, use_graph: bool = True):
+                 chunk: int = 200, use_graph: bool = True, stall_round: int = STALL_ROUND,
+                 stall_gain: float = STALL_GAIN, floor_rms: float = FLOOR_RMS):
     """The precision form run to an RMS below its FP32 floor: every instance
-    iterates in FP32 until RMS < switch_rms, then continues from its fields in
-    the plain FP64 form until RMS < rms_tol; max_iter bounds the two phases
-    together. Returns (results, wall seconds, seconds of the FP32 phase). The
-    iteration is the reference's update in both phases; only the propagators'
-    precision changes at the hand-over."""
+    iterates in FP32 until it sits on the FP32 floor (RMS < switch_rms and no
+    longer falling by stall_gain per stall_round iterations, or RMS < floor_rms),
+    then continues from its fields in the plain FP64 form until RMS < rms_tol.
+    max_iter bounds each instance's two phases together. Returns (results, wall
+    seconds, seconds of the FP32 phase). The iteration is the reference's update
+    in both phases; only the propagators' precision changes at the hand-over."""
+    n = len(surfaces)
     t0 = time.perf_counter()
-    with make_batch(surfaces, inputs, "fp32", switch_rms, use_graph) as b:
-        r32 = b.run(max_iter, chunk)
-        handoff = [i for i, r in enumerate(r32) if r.converged and r.status == 0]
-        fields = {i: b.get_fields(i) for i in handoff}
+    used = [0] * n
+    last_rms = [float("inf")] * n
+    it_after = [0] * n
+    handed = {}                      # instance -> fields
+    out: List[Optional[FinishedResult]] = [None] * n
+    with make_batch(surfaces, inputs, "fp32", rms_tol, use_graph) as b:
+        active = set(range(n))
+        while active:
+            res = b.run(stall_round, chunk)
+            for i in list(active):
+                r = res[i]
+                used[i] += r.iterations
+                it_after[i] = r.iter
+                done = r.converged or r.status != 0 or used[i] >= max_iter
+                if not done and r.rms < switch_rms and (r.rms > stall_gain * last_rms[i] or r.rms < floor_rms):
+                    handed[i] = b.get_fields(i)
+                    _freeze(b, i)
+                    active.discard(i)
+                elif done:
+                    out[i] = FinishedResult(used[i], used[i], r.rms, r.free_energy, bool(r.converged), r.status)
+                    _freeze(b, i)
+                    active.discard(i)
+                last_rms[i] = r.rms
     t1 = time.perf_counter()
-    out = [FinishedResult(r.iterations, r.iterations, r.rms, r.free_energy, False, r.status) for r in r32]
-    if handoff:
-        sub = [surfaces[i] for i in handoff]
-        left = max_iter - min(r32[i].iterations for i in handoff)
+    if handed:
+        keys = sorted(handed)
+        sub = [surfaces[i] for i in keys]
         b64 = Batch(sub, precision="fp64", use_graph=use_graph, noise="device")
         try:
-            for k, i in enumerate(handoff):
-                b64.set_fields(k, fields[i])
+            for k, i in enumerate(keys):
+                b64.set_fields(k, handed[i])
                 b64.set_masks(k, inputs[i][1])
-                b64.set_iteration(k, r32[i].iter)
+                b64.set_iteration(k, it_after[i])
                 b64.set_rng(k, (11 + i, 22, 33))
                 b64.set_stop(k, rms_tol)
-            r64 = b64.run(max(1, left), chunk)
+            used64 = [0] * len(keys)
+            live = set(range(len(keys)))
+            last = None
+            while live:
+                last = b64.run(chunk, chunk)
+                for k in list(live):
+                    r = last[k]
+                    used64[k] += r.iterations
+                    if r.converged or r.status != 0 or used[keys[k]] + used64[k] >= max_iter:
+                        if not r.converged:
+                            _freeze(b64, k)   # this instance's own cap
+                        live.discard(k)
+            for k, i in enumerate(keys):
+                r = last[k]
+                total = used[i] + used64[k]
+                out[i] = FinishedResult(total, used[i], r.rms, r.free_energy, bool(r.converged) and total <= max_iter,
+                                        r.status)
         finally:
             b64.close()
-        for k, i in enumerate(handoff):
-            r = r64[k]
-            total = r32[i].iterations + r.iterations
-            out[i] = FinishedResult(total, r32[i].iterations, r.rms, r.free_energy,
-                                    bool(r.converged) and total <= max_iter, r.status)
     return out, time.perf_counter() - t0, t1 - t0
 
 
