@@ -160,21 +160,21 @@ def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: 
                 b64.set_stop(k, rms_tol)
             used64 = [0] * len(keys)
             live = set(range(len(keys)))
-            last = None
             while live:
-                last = b64.run(chunk, chunk)
+                res = b64.run(chunk, chunk)
                 for k in list(live):
-                    r = last[k]
+                    r = res[k]
                     used64[k] += r.iterations
                     if r.converged or r.status != 0 or used[keys[k]] + used64[k] >= max_iter:
+                        # the result as the instance leaves; a capped one is then frozen, and the
+                        # stop-at-any-RMS that freezes it must not count as convergence
+                        i = keys[k]
+                        total = used[i] + used64[k]
+                        out[i] = FinishedResult(total, used[i], r.rms, r.free_energy,
+                                                bool(r.converged) and total <= max_iter, r.status)
                         if not r.converged:
                             _freeze(b64, k)   # this instance's own cap
                         live.discard(k)
-            for k, i in enumerate(keys):
-                r = last[k]
-                total = used[i] + used64[k]
-                out[i] = FinishedResult(total, used[i], r.rms, r.free_energy, bool(r.converged) and total <= max_iter,
-                                        r.status)
         finally:
             b64.close()
     return out, time.perf_counter() - t0, t1 - t0
