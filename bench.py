@@ -311,15 +311,20 @@ def _sweep_form(sw, surfaces, inputs, precision: str, rms_tol: float, max_iter: 
             "final_rms": [float(r.rms) for r in res]}
 
 
+SWEEP_FORMS = ("fp32", "fp64", "fp32x2", "finish_fp32x2", "finish_fp64")
+
+
 def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, device: int, sync,
-                  keep_points: bool = False):
+                  keep_points: bool = False, forms=SWEEP_FORMS):
     """The 2D droplet sweep (n x n chi points, uneven grids and NS, seeded
     droplet starts) run to RMS < rms_tol or max_iter, every form timed to the
     end: converged solves/hour = converged instances / wall time.
     fp32: the precision form on all n x n points. subset: points on a diagonal
     walk of the chi grid in both forms, the plain FP64 form and the precision
     form on the same instances, the same start and the same stop rule; their
-    ratio is read against the >= 5x target."""
+    ratio is read against the >= 5x target. subset >= n*n takes every point.
+    forms: which of SWEEP_FORMS run on the subset (the finishing forms and the
+    double-float form alone only below the FP32 floor)."""
     sw = importlib.import_module(f"{PKG}.sweep")
     surfaces = srn.configs.sweep_surfaces(n, seed=3, sizes=sw.SWEEP_SIZES, ns_range=(64, 128))
     inputs = sw.sweep_inputs(surfaces)
@@ -333,33 +338,49 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
         idx = sorted({(j * n // subset) * n + (j % n) for j in range(subset)} & set(range(len(surfaces))))
         ss = [surfaces[i] for i in idx]
         si = [inputs[i] for i in idx]
-        f32 = _sweep_form(sw, ss, si, "fp32", rms_tol, max_iter, sync)
-        f64 = _sweep_form(sw, ss, si, "fp64", rms_tol, max_iter, sync)
+        full_set = len(idx) == len(surfaces)
+        f32 = full if full_set else _sweep_form(sw, ss, si, "fp32", rms_tol, max_iter, sync)
+        sub = {"points": "all" if full_set else idx, "fp32": f32,
+               "basis": "converged instances / wall time to the end, every form on the same instances"}
+        ran = [f32]
+        f64 = None
+        if "fp64" in forms:
+            f64 = _sweep_form(sw, ss, si, "fp64", rms_tol, max_iter, sync)
+            sub["fp64_plain"] = f64
+            sub["solves_per_hour_ratio_fp32_over_fp64"] = (f32["solves_per_hour"] / f64["solves_per_hour"]
+                                                           if f64["solves_per_hour"] > 0 else None)
+            ran.append(f64)
+        if rms_tol < sw.SWITCH_RMS and "fp32x2" in forms:
+            # the double-float form alone, from the start: its per-iteration cost against FP64
+            sub["fp32x2"] = _sweep_form(sw, ss, si, "fp32x2", rms_tol, max_iter, sync)
+            ran.append(sub["fp32x2"])
         if not keep_points:
-            for f in (f32, f64):
-                f.pop("final_rms")
-        out["subset"] = {"points": idx, "fp32": f32, "fp64_plain": f64,
-                         "solves_per_hour_ratio_fp32_over_fp64": f32["solves_per_hour"] / f64["solves_per_hour"]
-                         if f64["solves_per_hour"] > 0 else None,
-                         "basis": "converged instances / wall time to the end, both forms on the same instances"}
+            for f in ran:
+                f.pop("final_rms", None)
+        out["subset"] = sub
         if rms_tol < sw.SWITCH_RMS:
-            # below the FP32 floor: the precision form hands over to FP64 on its floor
-            sync()
-            res, wall, wall32 = sw.run_finished(ss, si, rms_tol, max_iter)
-            sync()
-            conv = int(sum(r.converged for r in res))
-            fin = {"handover": f"RMS < {sw.SWITCH_RMS:g} and falling by less than {1 - sw.STALL_GAIN:g} over "
-                               f"{sw.STALL_ROUND} iterations, or RMS < {sw.FLOOR_RMS:g}; max_iter per instance "
-                               f"over both phases",
-                   "converged": conv, "wall_s": wall, "fp32_phase_s": wall32,
-                   "solves_per_hour": conv * 3600.0 / wall,
-                   "iterations_median": float(np.median([r.iterations for r in res])),
-                   "fp32_iterations_median": float(np.median([r.iterations_fp32 for r in res]))}
-            if keep_points:
-                fin["final_rms"] = [float(r.rms) for r in res]
-            out["subset"]["fp32_fp64_finish"] = fin
-            out["subset"]["solves_per_hour_ratio_finish_over_fp64"] = (
-                fin["solves_per_hour"] / f64["solves_per_hour"] if f64["solves_per_hour"] > 0 else None)
+            # below the FP32 floor: the precision form hands over on its floor, to the
+            # double-float form (the library's finish) and, for comparison, to plain FP64
+            for finish in ("fp32x2", "fp64"):
+                if f"finish_{finish}" not in forms:
+                    continue
+                sync()
+                res, wall, wall32 = sw.run_finished(ss, si, rms_tol, max_iter, finish=finish)
+                sync()
+                conv = int(sum(r.converged for r in res))
+                fin = {"handover": f"RMS < {sw.SWITCH_RMS:g} and falling by less than {1 - sw.STALL_GAIN:g} over "
+                                   f"{sw.STALL_ROUND} iterations, or RMS < {sw.FLOOR_RMS:g}; max_iter per instance "
+                                   f"over both phases",
+                       "converged": conv, "wall_s": wall, "fp32_phase_s": wall32,
+                       "solves_per_hour": conv * 3600.0 / wall,
+                       "iterations_median": float(np.median([r.iterations for r in res])),
+                       "fp32_iterations_median": float(np.median([r.iterations_fp32 for r in res]))}
+                if keep_points:
+                    fin["final_rms"] = [float(r.rms) for r in res]
+                out["subset"][f"fp32_{finish}_finish"] = fin
+                if f64 is not None:
+                    out["subset"][f"solves_per_hour_ratio_{finish}_finish_over_fp64"] = (
+                        fin["solves_per_hour"] / f64["solves_per_hour"] if f64["solves_per_hour"] > 0 else None)
     return out
 
 
@@ -621,6 +642,8 @@ def main():
     ap.add_argument("--sweep-subset", type=int, default=16,
                     help="points of the sweep run in both forms to the end (0: precision form only)")
     ap.add_argument("--sweep-points", action="store_true", help="keep every point's final RMS in the sweep record")
+    ap.add_argument("--sweep-forms", default=",".join(SWEEP_FORMS),
+                    help="forms run on the sweep subset: fp32, fp64, fp32x2, finish_fp32x2, finish_fp64")
     ap.add_argument("--serve-requests", type=int, default=40, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=4.0, help="mean arrivals per second")
     ap.add_argument("--serve-tol", type=float, default=1e-4)
@@ -709,7 +732,8 @@ def main():
         args.sweep_n = args.serve_requests = 0
     if args.sweep_n > 0:
         line["sweep"] = measure_sweep(srn, args.sweep_n, args.sweep_tol, args.sweep_max_iter, args.sweep_subset,
-                                      local, sync, keep_points=args.sweep_points)
+                                      local, sync, keep_points=args.sweep_points,
+                                      forms=tuple(f for f in args.sweep_forms.split(",") if f))
     if args.serve_requests > 0:
         line["serving"] = measure_serving(srn, args.serve_requests, args.serve_rate, args.serve_tol,
                                           args.serve_max_iter, local, args.serve_winners)

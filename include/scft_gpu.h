@@ -96,6 +96,9 @@ typedef struct scft_ctx scft_ctx;
 
 #define SCFT_PREC_FP64 0 /* plain form: every kernel in FP64 (the drop-in) */
 #define SCFT_PREC_FP32 1 /* precision form: propagators FP32, reductions FP64 */
+#define SCFT_PREC_FP32X2 2 /* propagators in double-float arithmetic (pairs of FP32, ~48-bit
+                              significand, FP32 exponent range) on double-float slices,
+                              reductions FP64: the finishing form below the FP32 form's floor */
 
 #define SCFT_NOISE_HOST 0    /* caller passes noise arrays to scft_iterate */
 #define SCFT_NOISE_DRAND48 1 /* device replays the drand48 stream (funGaussDev) */
@@ -226,6 +229,8 @@ int scft_batch_set_masks(scft_batch *b, int instance, const double *mask3);
 int scft_batch_set_iteration(scft_batch *b, int instance, unsigned long iter);
 int scft_batch_set_rng(scft_batch *b, int instance, const unsigned short seed[3]);
 int scft_batch_set_stop(scft_batch *b, int instance, double rms_tol);
+/* Stop an instance now (scft_freeze on its context); scft_batch_set_iteration re-arms it. */
+int scft_batch_freeze(scft_batch *b, int instance);
 int scft_batch_get_fields(scft_batch *b, int instance, double *w14);
 int scft_batch_get_densities(scft_batch *b, int instance, double *phi13, double *phi_tot);
 /* Iterate every instance until it converges or has run max_iter iterations in

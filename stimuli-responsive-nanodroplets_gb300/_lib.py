@@ -25,6 +25,7 @@ ERRORS = {
 }
 PREC_FP64 = 0
 PREC_FP32 = 1
+PREC_FP32X2 = 2
 NOISE_HOST = 0
 NOISE_DRAND48 = 1
 
@@ -156,6 +157,7 @@ def lib() -> C.CDLL:
         "scft_batch_set_iteration": (I, [VP, I, UL]),
         "scft_batch_set_rng": (I, [VP, I, us3]),
         "scft_batch_set_stop": (I, [VP, I, D]),
+        "scft_batch_freeze": (I, [VP, I]),
         "scft_batch_get_fields": (I, [VP, I, dp]),
         "scft_batch_get_densities": (I, [VP, I, dp, dp]),
         "scft_batch_run": (I, [VP, I, I, P(CBatchResult)]),
@@ -218,4 +220,4 @@ def check(code: int, where: str) -> None:
 
 
 __all__ = ["lib", "CSurface", "CDerived", "COptions", "CIterOut", "CTiming", "CBatchResult", "check", "ScftError", "FIELDS",
-           "PREC_FP64", "PREC_FP32", "exported_symbols"]
+           "PREC_FP64", "PREC_FP32", "PREC_FP32X2", "exported_symbols"]

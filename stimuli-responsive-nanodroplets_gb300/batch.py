@@ -37,7 +37,7 @@ class Batch:
         arr = (L.CSurface * self.n)(*[L.CSurface.from_surface(s) for s in self.surfaces])
         opt = L.COptions()
         L.lib().scft_options_default(C.byref(opt))
-        opt.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[precision]
+        opt.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32, "fp32x2": L.PREC_FP32X2}[precision]
         opt.device = device
         opt.use_graph = int(bool(use_graph))
         opt.kernel_path = {"auto": 0, "passes": 1}[kernel_path]
@@ -90,6 +90,10 @@ class Batch:
 
     def set_stop(self, i: int, rms_tol: float):
         L.check(L.lib().scft_batch_set_stop(self._h, i, float(rms_tol)), "scft_batch_set_stop")
+
+    def freeze(self, i: int):
+        """Stop instance i now; set_iteration re-arms it."""
+        L.check(L.lib().scft_batch_freeze(self._h, i), "scft_batch_freeze")
 
     def get_fields(self, i: int) -> np.ndarray:
         w = np.empty((14, self.M[i]))

@@ -165,6 +165,12 @@ extern "C" int scft_batch_set_stop(scft_batch *b, int i, double rms_tol)
     return scft_set_stop(c_, s_, rms_tol);
 }
 
+extern "C" int scft_batch_freeze(scft_batch *b, int i)
+{
+    LOCATE(b, i);
+    return scft_freeze(c_, s_);
+}
+
 extern "C" int scft_batch_get_fields(scft_batch *b, int i, double *w14)
 {
     LOCATE(b, i);

@@ -256,10 +256,21 @@ static int upload(scft_ctx *c, void **dst, const std::vector<T> &v)
     return SCFT_OK;
 }
 
-/* Convert a double vector to the context precision and upload. */
+/* Convert a double vector to the context precision and upload: FP64 as is,
+ * FP32 rounded to nearest, FP32x2 as the pair (hi, lo) nearest each value
+ * (hi = fl32(v), lo = fl32(v - hi)). */
 static int upload_p(scft_ctx *c, void **dst, const std::vector<double> &v)
 {
-    if (c->psize == 8) return upload(c, dst, v);
+    if (c->opt.precision == SCFT_PREC_FP64) return upload(c, dst, v);
+    if (c->opt.precision == SCFT_PREC_FP32X2) {
+        std::vector<float> f(2 * v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+            const float hi = (float)v[i];
+            f[2 * i] = hi;
+            f[2 * i + 1] = (float)(v[i] - (double)hi);
+        }
+        return upload(c, dst, f);
+    }
     std::vector<float> f(v.begin(), v.end());
     return upload(c, dst, f);
 }
@@ -763,7 +774,7 @@ static int autotune_axes(scft_ctx *c)
         const long lines = c->m / A.g.n;
         const long divisor = A.src == 2 ? lines : A.g.inner;
         char key[160];
-        snprintf(key, sizeof(key), "%d|%d,%d,%d,%d,%d|%d|%d", c->psize, A.g.n, A.g.ls, A.g.inner, A.g.outer,
+        snprintf(key, sizeof(key), "%d|%d,%d,%d,%d,%d|%d|%d", c->opt.precision, A.g.n, A.g.ls, A.g.inner, A.g.outer,
                  A.g.dirichlet, total, ai == 0 ? 1 : (ai == npass - 1 ? 2 : 0));
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1015,7 +1026,8 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     else
         scft_options_default(&opt);
     if (opt.n_instances < 1) opt.n_instances = 1;
-    if (opt.precision != SCFT_PREC_FP64 && opt.precision != SCFT_PREC_FP32) return SCFT_ERR_PARAM;
+    if (opt.precision != SCFT_PREC_FP64 && opt.precision != SCFT_PREC_FP32 && opt.precision != SCFT_PREC_FP32X2)
+        return SCFT_ERR_PARAM;
     if (opt.noise_mode != SCFT_NOISE_HOST && opt.noise_mode != SCFT_NOISE_DRAND48) {
         set_err("unknown noise_mode %d", opt.noise_mode);
         return SCFT_ERR_PARAM;
@@ -1030,7 +1042,7 @@ extern "C" int scft_ctx_create(const scft_surface *surfaces, const scft_options 
     scft_ctx *c = new scft_ctx();
     c->opt = opt;
     c->B = opt.n_instances;
-    c->psize = opt.precision == SCFT_PREC_FP64 ? 8 : 4;
+    c->psize = opt.precision == SCFT_PREC_FP32 ? 4 : 8; /* FP64, or an FP32 pair */
     c->device = opt.device;
     cudaSetDevice(opt.device);
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, opt.device);

@@ -200,6 +200,7 @@ int main(void)
     scft_options_default(&opt);
     const char *prec = getenv("SCFT_GB300_PRECISION");
     if (prec && strcmp(prec, "fp32") == 0) opt.precision = SCFT_PREC_FP32;
+    if (prec && strcmp(prec, "fp32x2") == 0) opt.precision = SCFT_PREC_FP32X2;
     const char *nm = getenv("SCFT_GB300_NOISE");
     const int host_noise = nm && strcmp(nm, "host") == 0;
     opt.noise_mode = host_noise ? SCFT_NOISE_HOST : SCFT_NOISE_DRAND48;

@@ -57,7 +57,7 @@ extern "C" int scft_propagate_static(scft_ctx *ctx, const double *q0, const doub
     const InstOps *ops = nullptr;
     scft_ctx_info(ctx, &dev, &prec, &m, &sm, &ds, &st, &ops);
     if (dev < 0 || dev >= SCFT_STATIC_MAX_DEVICES) return SCFT_ERR_PARAM;
-    const size_t psize = prec == SCFT_PREC_FP64 ? 8 : 4;
+    const size_t psize = prec == SCFT_PREC_FP32 ? 4 : 8; /* FP64 or an FP32 pair */
     const size_t slices = (size_t)steps + 1;
     /* layout: descriptor | FP64 staging of q (slices) | q in the context precision
      * (slices) | intermediate slice | Boltzmann slice | FP64 staging of w */

@@ -8,6 +8,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
+#include "scft_dfloat.cuh"
 #include "scft_internal.h"
 
 #define POST_THREADS 256
@@ -76,7 +79,7 @@ __device__ __forceinline__ P boltz(double ds, double w)
     if constexpr (sizeof(P) == 4)
         return 1.0f + expm1f((float)arg);
     else
-        return exp(arg);
+        return P(exp(arg)); /* FP64, or the FP32 pair nearest the FP64 value */
 }
 
 /* b for the fields chains use, and the initial slice of every chain: 1, the
@@ -182,6 +185,14 @@ struct AccF {
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+/* FP32x2 form: products of double-float slices, compensated double-float sums */
+struct AccDF {
+    DotDF d;
+    __device__ __forceinline__ void zero() { d.zero(); }
+    __device__ __forceinline__ void add(dfloat x, dfloat y) { d.add(x, y); }
+    __device__ __forceinline__ double value() const { return (double)d.hi + (double)d.lo; }
+};
+
 template <typename P>
 struct AccOf;
 template <>
@@ -192,11 +203,19 @@ template <>
 struct AccOf<float> {
     using T = AccF;
 };
+template <>
+struct AccOf<dfloat> {
+    using T = AccDF;
+};
 
 template <typename P, int V>
 __device__ __forceinline__ void load_p(const P *p, P (&o)[V])
 {
-    if (V == 4) {
+    if constexpr (std::is_same<P, dfloat>::value) {
+        const float4 t = *reinterpret_cast<const float4 *>(p); /* two double-float values */
+        o[0] = P(t.x, t.y);
+        o[1] = P(t.z, t.w);
+    } else if (V == 4) {
         const float4 t = *reinterpret_cast<const float4 *>(p);
         reinterpret_cast<float *>(o)[0] = t.x;
         reinterpret_cast<float *>(o)[1] = t.y;
@@ -573,6 +592,8 @@ cudaError_t scft_post_iter_begin(const PostArgs &a, int prec, int sms, cudaStrea
     dim3 g(grid_for(a.m, sms), a.B);
     if (prec == SCFT_PREC_FP64)
         k_boltz_init<double><<<g, POST_THREADS, 0, st>>>(a);
+    else if (prec == SCFT_PREC_FP32X2)
+        k_boltz_init<dfloat><<<g, POST_THREADS, 0, st>>>(a);
     else
         k_boltz_init<float><<<g, POST_THREADS, 0, st>>>(a);
     return cudaGetLastError();
@@ -588,10 +609,12 @@ int scft_post_nparts(long m, int sms) { return grid_for(m, sms); }
 
 cudaError_t scft_density_launch(const PostArgs &a, int prec, int sms, cudaStream_t st)
 {
-    const int vw = prec == SCFT_PREC_FP64 ? 2 : 4;
+    const int vw = prec == SCFT_PREC_FP32 ? 4 : 2;
     dim3 gd(grid_for((a.m + vw - 1) / vw, sms), a.nblocks, a.B);
     if (prec == SCFT_PREC_FP64)
         k_density<double><<<gd, POST_THREADS, 0, st>>>(a);
+    else if (prec == SCFT_PREC_FP32X2)
+        k_density<dfloat><<<gd, POST_THREADS, 0, st>>>(a);
     else
         k_density<float><<<gd, POST_THREADS, 0, st>>>(a);
     return cudaGetLastError();
@@ -603,13 +626,17 @@ cudaError_t scft_post_iter_end(const PostArgs &a, int prec, int sms, cudaStream_
     dim3 gq(gp, SCFT_NSPECIES, a.B);
     if (prec == SCFT_PREC_FP64)
         k_q_partial<double><<<gq, POST_THREADS, 0, st>>>(a);
+    else if (prec == SCFT_PREC_FP32X2)
+        k_q_partial<dfloat><<<gq, POST_THREADS, 0, st>>>(a);
     else
         k_q_partial<float><<<gq, POST_THREADS, 0, st>>>(a);
     k_q_final<<<dim3(SCFT_NSPECIES, a.B), 32, 0, st>>>(a, gp);
-    const int vw = prec == SCFT_PREC_FP64 ? 2 : 4;
+    const int vw = prec == SCFT_PREC_FP32 ? 4 : 2;
     dim3 gd(grid_for((a.m + vw - 1) / vw, sms), a.nblocks, a.B);
     if (prec == SCFT_PREC_FP64)
         k_density<double><<<gd, POST_THREADS, 0, st>>>(a);
+    else if (prec == SCFT_PREC_FP32X2)
+        k_density<dfloat><<<gd, POST_THREADS, 0, st>>>(a);
     else
         k_density<float><<<gd, POST_THREADS, 0, st>>>(a);
     {
@@ -663,6 +690,11 @@ cudaError_t scft_convert(int prec, const double *src, void *dst, long n, int to_
             k_d2p<double><<<g, 256, 0, st>>>(src, (double *)dst, n);
         else
             k_p2d<double><<<g, 256, 0, st>>>((const double *)src, (double *)dst, n);
+    } else if (prec == SCFT_PREC_FP32X2) {
+        if (to_p)
+            k_d2p<dfloat><<<g, 256, 0, st>>>(src, (dfloat *)dst, n);
+        else
+            k_p2d<dfloat><<<g, 256, 0, st>>>((const dfloat *)(const void *)src, (double *)dst, n);
     } else {
         if (to_p)
             k_d2p<float><<<g, 256, 0, st>>>(src, (float *)dst, n);
@@ -677,6 +709,8 @@ cudaError_t scft_boltz_one(int prec, const double *w, void *bz, double ds, long 
     const int g = (int)((m + 255) / 256 > 4096 ? 4096 : (m + 255) / 256);
     if (prec == SCFT_PREC_FP64)
         k_boltz1<double><<<g, 256, 0, st>>>(w, (double *)bz, ds, m);
+    else if (prec == SCFT_PREC_FP32X2)
+        k_boltz1<dfloat><<<g, 256, 0, st>>>(w, (dfloat *)bz, ds, m);
     else
         k_boltz1<float><<<g, 256, 0, st>>>(w, (float *)bz, ds, m);
     return cudaGetLastError();

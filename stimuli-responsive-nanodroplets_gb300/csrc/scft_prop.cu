@@ -18,9 +18,15 @@
  * Each pass is one launch over (line tile, chain) for every chain of every
  * instance that is active at contour step s; the first pass multiplies by b
  * on load, the last multiplies by b on store and writes slice s+1.
+ *
+ * The kernels are written once over the value type P: double (plain form),
+ * float (per-axis passes of the FP32 form) and dfloat (the FP32x2 form: slices,
+ * Boltzmann factors and operator tables stored as FP32 pairs, every operation
+ * in double-float arithmetic, no FP64 instruction on the contour path).
  */
 #include <cuda_runtime.h>
 
+#include "scft_dfloat.cuh"
 #include "scft_internal.h"
 
 template <typename P>
@@ -32,6 +38,12 @@ template <typename P>
 __device__ __forceinline__ Cx<P> cmul(Cx<P> a, Cx<P> b)
 {
     return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+/* double-float complex product: each part is one two-product difference with a
+ * single renormalisation */
+__device__ __forceinline__ Cx<dfloat> cmul(Cx<dfloat> a, Cx<dfloat> b)
+{
+    return {dfo::mul_sub(a.x, b.x, a.y, b.y), dfo::mul_add(a.x, b.y, a.y, b.x)};
 }
 template <typename P>
 __device__ __forceinline__ Cx<P> cadd(Cx<P> a, Cx<P> b) { return {a.x + b.x, a.y + b.y}; }
@@ -133,6 +145,24 @@ __device__ Cx<P> *stockham(Cx<P> *a, Cx<P> *b, int n, int ldl, int nl, const Axi
 }
 
 
+
+/* Dot-product accumulator of the dense z pass: a plain multiply-add chain in
+ * FP32 and FP64 (the expression the plain form has always used), the
+ * compensated double-float accumulator for dfloat. */
+template <typename P>
+struct DotOf {
+    P s;
+    __device__ __forceinline__ void zero() { s = (P)0; }
+    __device__ __forceinline__ void add(P a, P b) { s += a * b; }
+    __device__ __forceinline__ P value() const { return s; }
+};
+template <>
+struct DotOf<dfloat> {
+    DotDF d;
+    __device__ __forceinline__ void zero() { d.zero(); }
+    __device__ __forceinline__ void add(dfloat a, dfloat b) { d.add(a, b); }
+    __device__ __forceinline__ dfloat value() const { return d.value(); }
+};
 
 template <typename P>
 __device__ __forceinline__ long elem_offset(const AxisGeom &g, long L, int t)
@@ -277,14 +307,17 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
             const int l = e / h, i = e - l * h;
             const P *ul = u + l * h;
             const P *vl = v + l * h;
-            P sacc = 0, dacc = 0;
+            DotOf<P> sacc, dacc;
+            sacc.zero();
+            dacc.zero();
             for (int j = 0; j < h; ++j) {
-                sacc += kA[j * h + i] * ul[j];
-                dacc += kB[j * h + i] * vl[j];
+                sacc.add(kA[j * h + i], ul[j]);
+                dacc.add(kB[j * h + i], vl[j]);
             }
             const long o0 = elem_offset<P>(g, L0 + l, i);
             const long o1 = elem_offset<P>(g, L0 + l, n - 1 - i);
-            P y0 = sacc + dacc, y1 = sacc - dacc;
+            const P sv = sacc.value(), dv = dacc.value();
+            P y0 = sv + dv, y1 = sv - dv;
             if (a.last) {
                 y0 *= bz[o0];
                 y1 *= bz[o1];
@@ -296,8 +329,10 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
         for (int e = threadIdx.x; e < a.tile * n; e += blockDim.x) {
             const int l = e / n, i = e - l * n;
             const P *xl = x + l * n;
-            P acc = 0;
-            for (int j = 0; j < n; ++j) acc += kA[j * n + i] * xl[j];
+            DotOf<P> dot;
+            dot.zero();
+            for (int j = 0; j < n; ++j) dot.add(kA[j * n + i], xl[j]);
+            P acc = dot.value();
             const long o0 = elem_offset<P>(g, L0 + l, i);
             if (a.last) acc *= bz[o0];
             dst[o0] = acc;
@@ -330,7 +365,9 @@ static cudaError_t launch_pass_t(const AxisGeom &g, const PassArgs &a, int ntile
 
 cudaError_t scft_launch_pass(int prec, const AxisGeom &g, const PassArgs &a, int ntiles, cudaStream_t st)
 {
-    return prec == SCFT_PREC_FP64 ? launch_pass_t<double>(g, a, ntiles, st) : launch_pass_t<float>(g, a, ntiles, st);
+    if (prec == SCFT_PREC_FP64) return launch_pass_t<double>(g, a, ntiles, st);
+    if (prec == SCFT_PREC_FP32X2) return launch_pass_t<dfloat>(g, a, ntiles, st);
+    return launch_pass_t<float>(g, a, ntiles, st);
 }
 
 /* Raise the dynamic shared-memory limit of the pass kernels once, outside any
@@ -343,5 +380,7 @@ cudaError_t scft_pass_configure(int smem_bytes)
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pass_fft<float>, A, smem_bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pass_dense<double>, A, smem_bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pass_dense<float>, A, smem_bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pass_fft<dfloat>, A, smem_bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pass_dense<dfloat>, A, smem_bytes);
     return e;
 }

@@ -1200,12 +1200,12 @@ static cudaError_t launch_t(const Step2DArgs &a, int nblocks, cudaStream_t st, i
 
 /* Returns the shared-memory bytes of the fused step for (nx, nz) in this
  * precision, or 0 if the shape has no fused kernel. Only the FP32 form has
- * one: an FP64 row pair does not fit in registers, and the FP64 form is bound
- * by the FP64 units, so it keeps the per-axis passes. */
+ * one: an FP64 or double-float row pair does not fit in registers, and those
+ * forms are bound by arithmetic, so they keep the per-axis passes. */
 size_t scft_step2d_smem(int prec, int nx, int nz)
 {
 #define X(NX_, NZ_, A_, B_)                                                                                           \
-    if (nx == NX_ && nz == NZ_) return prec == SCFT_PREC_FP64 ? 0 : smem_bytes_t<float, NX_, NZ_, A_, B_>();
+    if (nx == NX_ && nz == NZ_) return prec != SCFT_PREC_FP32 ? 0 : smem_bytes_t<float, NX_, NZ_, A_, B_>();
     SCFT_STEP2D_SHAPES(X)
 #undef X
     return 0;
@@ -1216,7 +1216,7 @@ size_t scft_step2d_smem(int prec, int nx, int nz)
  * and the bf16 pieces, not the FP32 halves). */
 int scft_step2d_ztc(int prec, int nx, int nz)
 {
-    if (prec == SCFT_PREC_FP64) return 0;
+    if (prec != SCFT_PREC_FP32) return 0;
 #define X(NX_, NZ_, A_, B_) \
     if (nx == NX_ && nz == NZ_) return ZTcOk<float, NX_, NZ_>::value ? 1 : 0;
     SCFT_STEP2D_SHAPES(X)
@@ -1228,7 +1228,7 @@ int scft_step2d_ztc(int prec, int nx, int nz)
  * for batches of at most one chain per SM). */
 int scft_step2d_wide(int prec, int nx, int nz)
 {
-    if (prec == SCFT_PREC_FP64) return 0;
+    if (prec != SCFT_PREC_FP32) return 0;
 #define X(NX_, NZ_, A_, B_) \
     if (nx == NX_ && nz == NZ_) return WideOk<NX_, NZ_>::value ? 1 : 0;
     SCFT_STEP2D_SHAPES(X)
@@ -1244,7 +1244,7 @@ cudaError_t scft_launch_step2d(int prec, int nx, int nz, const Step2DArgs &a, in
 {
 #define X(NX_, NZ_, A_, B_)                                                                                           \
     if (nx == NX_ && nz == NZ_)                                                                                        \
-        return prec == SCFT_PREC_FP64 ? cudaErrorInvalidValue                                                         \
+        return prec != SCFT_PREC_FP32 ? cudaErrorInvalidValue                                                         \
                                       : launch_t<float, NX_, NZ_, A_, B_>(a, nblocks, st, configure, wide);
     SCFT_STEP2D_SHAPES(X)
 #undef X

@@ -91,8 +91,10 @@ def _us3(seed) -> C.Array:
 class Solver:
     """One GPU context for ``len(surfaces)`` SCFT instances of one shape.
 
-    precision: "fp64" (plain form, the drop-in) or "fp32" (FP32 propagators,
-    FP64 densities/Q/free energy/update).
+    precision: "fp64" (plain form, the drop-in), "fp32" (FP32 propagators,
+    FP64 densities/Q/free energy/update) or "fp32x2" (propagators in
+    double-float arithmetic, pairs of FP32 with ~48 significant bits, FP64
+    reductions: the finishing form below the FP32 form's RMS floor).
     noise: "host" (the caller passes the drand48 draws to iterate) or "device"
     (the library replays the drand48 stream itself from set_rng's state).
     """
@@ -106,7 +108,7 @@ class Solver:
         arr = (L.CSurface * self.B)(*[L.CSurface.from_surface(s) for s in self.surfaces])
         opt = L.COptions()
         L.lib().scft_options_default(C.byref(opt))
-        opt.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[precision]
+        opt.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32, "fp32x2": L.PREC_FP32X2}[precision]
         opt.device = device
         opt.use_graph = int(bool(use_graph))
         opt.n_instances = self.B

@@ -9,6 +9,8 @@ which solves/hour follows.
 """
 from __future__ import annotations
 
+import queue
+import threading
 import time
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
@@ -113,71 +115,116 @@ def _freeze(b: Batch, i: int):
 
 def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: int, switch_rms: float = SWITCH_RMS,
                  chunk: int = 200, use_graph: bool = True, stall_round: int = STALL_ROUND,
-                 stall_gain: float = STALL_GAIN, floor_rms: float = FLOOR_RMS):
+                 stall_gain: float = STALL_GAIN, floor_rms: float = FLOOR_RMS, finish: str = "fp32x2"):
     """The precision form run to an RMS below its FP32 floor: every instance
     iterates in FP32 until it sits on the FP32 floor (RMS < switch_rms and no
     longer falling by stall_gain per stall_round iterations, or RMS < floor_rms),
-    then continues from its fields in the plain FP64 form until RMS < rms_tol.
-    max_iter bounds each instance's two phases together. Returns (results, wall
-    seconds, seconds of the FP32 phase). The iteration is the reference's update
-    in both phases; only the propagators' precision changes at the hand-over."""
+    then continues from its fields in the `finish` form until RMS < rms_tol:
+    "fp32x2" (double-float propagators, ~48 significant bits, several times
+    faster than FP64 on GB300) or "fp64" (the plain form). max_iter bounds each
+    instance's two phases together. The iteration is the reference's update in
+    both phases; only the propagators' precision changes at the hand-over.
+
+    The two phases overlap: the finishing batch (every instance, each frozen
+    until it is handed over) is driven by a second host thread, which arms
+    instances between its rounds as the FP32 batch hands them over, so
+    finishing starts while the FP32 batch still runs its slower instances.
+    The two batches are separate contexts on their own streams. Returns
+    (results, wall seconds, seconds of the FP32 phase), timed from the first
+    iteration (batch creation excluded, as in the single-form runs)."""
     n = len(surfaces)
-    t0 = time.perf_counter()
     used = [0] * n
     last_rms = [float("inf")] * n
-    it_after = [0] * n
-    handed = {}                      # instance -> fields
     out: List[Optional[FinishedResult]] = [None] * n
-    with make_batch(surfaces, inputs, "fp32", rms_tol, use_graph) as b:
-        active = set(range(n))
-        while active:
-            res = b.run(stall_round, chunk)
-            for i in list(active):
-                r = res[i]
-                used[i] += r.iterations
-                it_after[i] = r.iter
-                done = r.converged or r.status != 0 or used[i] >= max_iter
-                if not done and r.rms < switch_rms and (r.rms > stall_gain * last_rms[i] or r.rms < floor_rms):
-                    handed[i] = b.get_fields(i)
-                    _freeze(b, i)
-                    active.discard(i)
-                elif done:
-                    out[i] = FinishedResult(used[i], used[i], r.rms, r.free_energy, bool(r.converged), r.status)
-                    _freeze(b, i)
-                    active.discard(i)
-                last_rms[i] = r.rms
-    t1 = time.perf_counter()
-    if handed:
-        keys = sorted(handed)
-        sub = [surfaces[i] for i in keys]
-        b64 = Batch(sub, precision="fp64", use_graph=use_graph, noise="device")
+    handq: "queue.Queue" = queue.Queue()
+    errors: list = []
+    b = make_batch(surfaces, inputs, "fp32", rms_tol, use_graph)
+    bf = None
+    try:
+        bf = Batch(surfaces, precision=finish, use_graph=use_graph, noise="device")
+        for i, (w, m) in enumerate(inputs):
+            bf.set_fields(i, w)          # placeholders until the hand-over brings the FP32 fields
+            bf.set_masks(i, m)
+            bf.freeze(i)
+
+        def finisher():
+            live = {}                    # instance -> FP32 iterations it ran
+            ran = {}                     # instance -> iterations in the finishing form
+            fp32_over = False
+            try:
+                while True:
+                    pending = []
+                    if not live and not fp32_over:
+                        pending.append(handq.get())          # idle: wait for the next hand-over
+                    while True:
+                        try:
+                            pending.append(handq.get_nowait())
+                        except queue.Empty:
+                            break
+                    for item in pending:
+                        if item is None:
+                            fp32_over = True
+                            continue
+                        i, w, it_after, used32 = item
+                        bf.set_fields(i, w)
+                        bf.set_iteration(i, it_after)       # re-arms the frozen instance
+                        bf.set_rng(i, (11 + i, 22, 33))
+                        bf.set_stop(i, rms_tol)
+                        live[i] = used32
+                        ran[i] = 0
+                    if not live:
+                        if fp32_over:
+                            return
+                        continue
+                    res = bf.run(chunk, chunk)
+                    for i in list(live):
+                        r = res[i]
+                        ran[i] += r.iterations
+                        total = live[i] + ran[i]
+                        if r.converged or r.status != 0 or total >= max_iter:
+                            # the result as the instance leaves; a capped one is frozen here,
+                            # so its stop is never mistaken for convergence
+                            out[i] = FinishedResult(total, live[i], r.rms, r.free_energy,
+                                                    bool(r.converged) and total <= max_iter, r.status)
+                            if not r.converged:
+                                bf.freeze(i)
+                            del live[i]
+            except BaseException as e:                     # reported by the caller
+                errors.append(e)
+
+        t0 = time.perf_counter()
+        th = threading.Thread(target=finisher, name="fp32-finish", daemon=True)
+        th.start()
         try:
-            for k, i in enumerate(keys):
-                b64.set_fields(k, handed[i])
-                b64.set_masks(k, inputs[i][1])
-                b64.set_iteration(k, it_after[i])
-                b64.set_rng(k, (11 + i, 22, 33))
-                b64.set_stop(k, rms_tol)
-            used64 = [0] * len(keys)
-            live = set(range(len(keys)))
-            while live:
-                res = b64.run(chunk, chunk)
-                for k in list(live):
-                    r = res[k]
-                    used64[k] += r.iterations
-                    if r.converged or r.status != 0 or used[keys[k]] + used64[k] >= max_iter:
-                        # the result as the instance leaves; a capped one is then frozen, and the
-                        # stop-at-any-RMS that freezes it must not count as convergence
-                        i = keys[k]
-                        total = used[i] + used64[k]
-                        out[i] = FinishedResult(total, used[i], r.rms, r.free_energy,
-                                                bool(r.converged) and total <= max_iter, r.status)
-                        if not r.converged:
-                            _freeze(b64, k)   # this instance's own cap
-                        live.discard(k)
+            active = set(range(n))
+            while active:
+                res = b.run(stall_round, chunk)
+                for i in list(active):
+                    r = res[i]
+                    used[i] += r.iterations
+                    done = r.converged or r.status != 0 or used[i] >= max_iter
+                    if not done and r.rms < switch_rms and (r.rms > stall_gain * last_rms[i] or r.rms < floor_rms):
+                        handq.put((i, b.get_fields(i), r.iter, used[i]))
+                        _freeze(b, i)
+                        active.discard(i)
+                    elif done:
+                        out[i] = FinishedResult(used[i], used[i], r.rms, r.free_energy, bool(r.converged), r.status)
+                        _freeze(b, i)
+                        active.discard(i)
+                    last_rms[i] = r.rms
+                if errors:
+                    break
+            t1 = time.perf_counter()
         finally:
-            b64.close()
-    return out, time.perf_counter() - t0, t1 - t0
+            handq.put(None)
+            th.join()
+        if errors:
+            raise errors[0]
+        return out, time.perf_counter() - t0, t1 - t0
+    finally:
+        b.close()
+        if bf is not None:
+            bf.close()
 
 
 def summary(run: SweepRun) -> dict:

@@ -25,17 +25,19 @@ def test_small_sweep_runs_to_tolerance(srn):
     assert st["converged"] >= 1
 
 
-def test_fp32_with_fp64_finish_reaches_the_fp64_fixed_point(srn):
+@pytest.mark.parametrize("finish", ["fp32x2", "fp64"])
+def test_fp32_with_finish_reaches_the_fp64_fixed_point(srn, finish):
     """Below the FP32 form's RMS floor the precision form hands each instance
-    over to the plain FP64 form: it converges to the tolerance, to the free
-    energy the plain FP64 form reaches on its own (1e-6 relative), having run
-    its first iterations in FP32, within its own iteration cap."""
+    over to a finishing form (double-float or plain FP64 propagators): it
+    converges to the tolerance, to the free energy the plain FP64 form reaches
+    on its own (1e-6 relative), having run its first iterations in FP32,
+    within its own iteration cap."""
     cfg = srn.configs
     surfaces = cfg.sweep_surfaces(2, seed=1, sizes=((32, 16), (48, 16)), ns_range=(40, 60))
     inputs = sweep.sweep_inputs(surfaces)
     # hand-over forced above the tolerance (floor_rms), so both phases run
     res, wall, wall32 = sweep.run_finished(surfaces, inputs, rms_tol=1e-5, max_iter=8000, switch_rms=1e-4,
-                                           floor_rms=5e-5)
+                                           floor_rms=5e-5, finish=finish)
     with sweep.make_batch(surfaces, inputs, "fp64", 1e-5) as b:
         ref = b.run(8000, chunk=200)
     assert 0 < wall32 < wall
