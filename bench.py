@@ -308,7 +308,7 @@ def _sweep_form(sw, surfaces, inputs, precision: str, rms_tol: float, max_iter: 
             "solves_per_hour": conv * 3600.0 / wall, "iterations_median": float(np.median(its)),
             "iterations_max": int(its.max()), "instance_iterations_per_s": float(its.sum()) / wall,
             "nonfinite": int(sum(r.status != 0 for r in res)), "by_shape": by_shape,
-            "final_rms": [float(r.rms) for r in res]}
+            "final_rms": [float(r.rms) for r in res], "final_free_energy": [float(r.free_energy) for r in res]}
 
 
 SWEEP_FORMS = ("fp32", "fp64", "fp32x2", "finish_fp32x2", "finish_fp64")
@@ -329,8 +329,10 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
     surfaces = srn.configs.sweep_surfaces(n, seed=3, sizes=sw.SWEEP_SIZES, ns_range=(64, 128))
     inputs = sw.sweep_inputs(surfaces)
     full = _sweep_form(sw, surfaces, inputs, "fp32", rms_tol, max_iter, sync)
+    full_F, full_rms = list(full["final_free_energy"]), list(full["final_rms"])
     if not keep_points:
         full.pop("final_rms")
+        full.pop("final_free_energy")
     out = {"rms_tol": rms_tol, "max_iter": max_iter, "fp32": full}
     if subset > 0:
         # spread over both chi axes: point j sits in row j*n/subset of the grid,
@@ -340,12 +342,20 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
         si = [inputs[i] for i in idx]
         full_set = len(idx) == len(surfaces)
         f32 = full if full_set else _sweep_form(sw, ss, si, "fp32", rms_tol, max_iter, sync)
+        f32_F = full_F if full_set else list(f32["final_free_energy"])
+        f32_conv = [r < rms_tol for r in (full_rms if full_set else f32["final_rms"])]
         sub = {"points": "all" if full_set else idx, "fp32": f32,
                "basis": "converged instances / wall time to the end, every form on the same instances"}
         ran = [f32]
         f64 = None
         if "fp64" in forms:
             f64 = _sweep_form(sw, ss, si, "fp64", rms_tol, max_iter, sync)
+            f64_F = list(f64["final_free_energy"])
+            f64_conv = [r < rms_tol for r in f64["final_rms"]]
+            both = [k for k in range(len(ss)) if f64_conv[k] and f32_conv[k]]
+            sub["fp32_vs_fp64_converged_in_both"] = len(both)
+            sub["fp32_vs_fp64_max_rel_free_energy_diff"] = max(
+                (abs(f32_F[k] - f64_F[k]) / abs(f64_F[k]) for k in both), default=None)
             sub["fp64_plain"] = f64
             sub["solves_per_hour_ratio_fp32_over_fp64"] = (f32["solves_per_hour"] / f64["solves_per_hour"]
                                                            if f64["solves_per_hour"] > 0 else None)
@@ -357,6 +367,7 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
         if not keep_points:
             for f in ran:
                 f.pop("final_rms", None)
+                f.pop("final_free_energy", None)
         out["subset"] = sub
         if rms_tol < sw.SWITCH_RMS:
             # below the FP32 floor: the precision form hands over on its floor, to the
@@ -377,6 +388,13 @@ def measure_sweep(srn, n: int, rms_tol: float, max_iter: int, subset: int, devic
                        "fp32_iterations_median": float(np.median([r.iterations_fp32 for r in res]))}
                 if keep_points:
                     fin["final_rms"] = [float(r.rms) for r in res]
+                    fin["final_free_energy"] = [float(r.free_energy) for r in res]
+                if f64 is not None:
+                    # converged in both: the finish form's free energy against the plain FP64 form's
+                    both = [k for k, r in enumerate(res) if r.converged and f64_conv[k]]
+                    fin["converged_in_both"] = len(both)
+                    fin["max_rel_free_energy_diff_vs_fp64"] = max(
+                        (abs(res[k].free_energy - f64_F[k]) / abs(f64_F[k]) for k in both), default=None)
                 out["subset"][f"fp32_{finish}_finish"] = fin
                 if f64 is not None:
                     out["subset"][f"solves_per_hour_ratio_{finish}_finish_over_fp64"] = (
@@ -635,7 +653,7 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=0,
                     help="cap on the reference arm's timed (and warm-up) steps; 0: run --steps as given")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "fp32x2"])
     ap.add_argument("--sweep-n", type=int, default=16, help="n x n chi points of the droplet sweep (0: skip)")
     ap.add_argument("--sweep-tol", type=float, default=1e-4)
     ap.add_argument("--sweep-max-iter", type=int, default=5000)
@@ -652,7 +670,8 @@ def main():
                     help="points of the FP32-vs-FP64 lowest-F winner check after serving (0: skip)")
     ap.add_argument("--profile-iters", type=int, default=1, help="iterations of --profile-case")
     ap.add_argument("--profile-case", action="store_true",
-                    help="one iteration of one form only (for ncu captures); prints no bench line")
+                    help="one iteration of one form only (for ncu captures; the iterations sit in a "
+                         "profiler range for --profile-from-start off); prints no bench line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -686,8 +705,11 @@ def main():
             if m is not None:
                 sv.set_masks(m, b)
             sv.set_iteration(start_iteration(s), b)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
         out = sv.iterate(args.profile_iters)
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         print(f"profile case: {len(surfaces)} instances, {args.profile_iters} iteration(s), "
               f"F[0] = {out[-1][0].free_energy:.12f}")
         sv.close()

@@ -33,6 +33,10 @@
 struct InstOps {
     const void *kz, *twx, *ex;
     const void *spec[3], *tw[3], *kA[3], *kB[3];
+    /* FP32x2 form, dense axes: per output row i the columns [lo, hi) outside of
+     * which every operator entry is below 2^-60 of the largest (int2 per row);
+     * NULL elsewhere */
+    const int2 *band[3];
 };
 
 /* One propagator chain of one instance: q[0] from init, then len-1 contour
@@ -108,6 +112,11 @@ struct AxisGeom {
     int dirichlet; /* 1: dense Dirichlet operator, 0: periodic FFT */
     int nrad;
     int rad[SCFT_MAX_RADIX_STAGES];
+    /* per stage: ceil(2^32 / d) for d = n / rad (the butterflies of a line) and
+     * d = the product of the earlier radices (0 when d = 1), so the Stockham
+     * stages divide by a multiply-high instead of an integer division */
+    unsigned mag_nr[SCFT_MAX_RADIX_STAGES];
+    unsigned mag_ns[SCFT_MAX_RADIX_STAGES];
 };
 
 /* Arguments of one axis pass of the propagator step (scft_prop.cu). */

@@ -26,6 +26,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "scft_dfloat.cuh"
 #include "scft_internal.h"
 
@@ -89,26 +91,33 @@ __device__ __forceinline__ void dft3(Cx<P> *v)
     v[2] = {c.x - h * e.x, c.y - h * e.y};
 }
 
+/* floor(x / d) for x * d < 2^32, given mag = ceil(2^32 / d) (0 for d = 1) */
+__device__ __forceinline__ int div_mag(int x, unsigned mag) { return mag ? (int)__umulhi((unsigned)x, mag) : x; }
+
 /* One Stockham autosort stage (Govindaraju et al., SC'08 formulation) over nl
- * complex lines of length n with line pitch ldl. tw[t] = exp(-2 pi i t / n). */
+ * complex lines of length n with line pitch ldl. tw[t] = exp(-2 pi i t / n).
+ * r * k * tws < n for every butterfly input, so the twiddle index needs no
+ * reduction modulo n. */
 template <typename P, bool INV, int R>
 __device__ __forceinline__ void stockham_stage(const Cx<P> *__restrict__ a, Cx<P> *__restrict__ b, int n, int ldl,
-                                               int nl, int Ns, const Cx<P> *__restrict__ tw)
+                                               int nl, int Ns, unsigned mag_nr, unsigned mag_ns,
+                                               const Cx<P> *__restrict__ tw)
 {
     const int nr = n / R;
     const int tws = n / (Ns * R);
     for (int w = threadIdx.x; w < nl * nr; w += blockDim.x) {
-        const int line = w / nr;
+        const int line = div_mag(w, mag_nr);
         const int j = w - line * nr;
         const Cx<P> *in = a + line * ldl;
         Cx<P> *out = b + line * ldl;
-        const int k = j % Ns;
+        const int jq = div_mag(j, mag_ns);
+        const int k = j - jq * Ns;
         Cx<P> v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             v[r] = in[j + r * nr];
             if (r > 0 && k > 0) {
-                Cx<P> t = tw[(r * k * tws) % n];
+                Cx<P> t = tw[r * k * tws];
                 if (INV) t.y = -t.y;
                 v[r] = cmul(v[r], t);
             }
@@ -116,7 +125,7 @@ __device__ __forceinline__ void stockham_stage(const Cx<P> *__restrict__ a, Cx<P
         if (R == 2) dft2<P, INV>(v);
         if (R == 3) dft3<P, INV>(v);
         if (R == 4) dft4<P, INV>(v);
-        const int base = (j / Ns) * Ns * R + k;
+        const int base = jq * Ns * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) out[base + r * Ns] = v[r];
     }
@@ -129,12 +138,13 @@ __device__ Cx<P> *stockham(Cx<P> *a, Cx<P> *b, int n, int ldl, int nl, const Axi
     int Ns = 1;
     for (int st = 0; st < g.nrad; ++st) {
         const int R = g.rad[st];
+        const unsigned mnr = g.mag_nr[st], mns = g.mag_ns[st];
         if (R == 4)
-            stockham_stage<P, INV, 4>(a, b, n, ldl, nl, Ns, tw);
+            stockham_stage<P, INV, 4>(a, b, n, ldl, nl, Ns, mnr, mns, tw);
         else if (R == 2)
-            stockham_stage<P, INV, 2>(a, b, n, ldl, nl, Ns, tw);
+            stockham_stage<P, INV, 2>(a, b, n, ldl, nl, Ns, mnr, mns, tw);
         else
-            stockham_stage<P, INV, 3>(a, b, n, ldl, nl, Ns, tw);
+            stockham_stage<P, INV, 3>(a, b, n, ldl, nl, Ns, mnr, mns, tw);
         __syncthreads();
         Cx<P> *t = a;
         a = b;
@@ -198,9 +208,9 @@ __global__ void __launch_bounds__(256) k_pass_fft(AxisGeom g, PassArgs a)
         tw[t] = gtw[t];
         spec[t] = gspec[t];
     }
-    const long L0 = (long)blockIdx.x * a.tile;
     const int total = a.tile * n;
     const bool contiguous = (g.ls == 1);
+    const long L0 = (long)blockIdx.x * a.tile;
     for (int e = threadIdx.x; e < nl * 2 * n; e += blockDim.x) {
         /* zero the imaginary half of a trailing unpaired line */
         const int l = e / n, t = e - l * n;
@@ -261,10 +271,13 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
     if (a.s >= cd.len - 1) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, h = a.h;
+    /* u and v rows have an odd pitch (h + 1 values): the two lines a warp can
+     * span then broadcast from different banks */
+    const int hp = h + 1;
     P *x = reinterpret_cast<P *>(smem_raw);   /* tile * n */
-    P *u = x + a.tile * n;                    /* tile * h */
-    P *v = u + a.tile * h;                    /* tile * h */
-    P *kA = v + a.tile * h;                   /* h * h */
+    P *u = x + a.tile * n;                    /* tile * hp */
+    P *v = u + a.tile * hp;                   /* tile * hp */
+    P *kA = v + a.tile * hp;                  /* h * h */
     P *kB = kA + h * h;                       /* h * h (even n) */
 
     const P *src = a.first ? reinterpret_cast<const P *>(cd.q) + (long)a.s * a.sstride
@@ -273,13 +286,15 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
     const P *bz = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
     const P *gA = reinterpret_cast<const P *>(cd.ops->kA[a.axis]);
     const P *gB = reinterpret_cast<const P *>(cd.ops->kB[a.axis]);
+    /* the band of nonnegligible columns per row (FP32x2 form only) */
+    const int2 *band = std::is_same<P, dfloat>::value ? cd.ops->band[a.axis] : nullptr;
     for (int e = threadIdx.x; e < h * h; e += blockDim.x) {
         kA[e] = gA[e];
         if (a.even) kB[e] = gB[e];
     }
-    const long L0 = (long)blockIdx.x * a.tile;
     const int total = a.tile * n;
     const bool contiguous = (g.ls == 1);
+    const long L0 = (long)blockIdx.x * a.tile;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
         int l, t;
         if (contiguous) {
@@ -299,18 +314,24 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
         for (int e = threadIdx.x; e < a.tile * h; e += blockDim.x) {
             const int l = e / h, i = e - l * h;
             const P p0 = x[l * n + i], p1 = x[l * n + n - 1 - i];
-            u[e] = p0 + p1;
-            v[e] = p0 - p1;
+            u[l * hp + i] = p0 + p1;
+            v[l * hp + i] = p0 - p1;
         }
         __syncthreads();
         for (int e = threadIdx.x; e < a.tile * h; e += blockDim.x) {
             const int l = e / h, i = e - l * h;
-            const P *ul = u + l * h;
-            const P *vl = v + l * h;
+            const P *ul = u + l * hp;
+            const P *vl = v + l * hp;
             DotOf<P> sacc, dacc;
             sacc.zero();
             dacc.zero();
-            for (int j = 0; j < h; ++j) {
+            int j0 = 0, j1 = h;
+            if (band) {
+                const int2 r = band[i];
+                j0 = r.x;
+                j1 = r.y;
+            }
+            for (int j = j0; j < j1; ++j) {
                 sacc.add(kA[j * h + i], ul[j]);
                 dacc.add(kB[j * h + i], vl[j]);
             }
@@ -331,7 +352,13 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
             const P *xl = x + l * n;
             DotOf<P> dot;
             dot.zero();
-            for (int j = 0; j < n; ++j) dot.add(kA[j * n + i], xl[j]);
+            int j0 = 0, j1 = n;
+            if (band) {
+                const int2 r = band[i];
+                j0 = r.x;
+                j1 = r.y;
+            }
+            for (int j = j0; j < j1; ++j) dot.add(kA[j * n + i], xl[j]);
             P acc = dot.value();
             const long o0 = elem_offset<P>(g, L0 + l, i);
             if (a.last) acc *= bz[o0];
@@ -345,7 +372,7 @@ size_t scft_pass_smem_bytes(const AxisGeom &g, int tile, int h, int psize)
 {
     if (g.dirichlet) {
         const int n = g.n;
-        return (size_t)psize * ((size_t)tile * n + 2 * (size_t)tile * h + 2 * (size_t)h * h);
+        return (size_t)psize * ((size_t)tile * n + 2 * (size_t)tile * (h + 1) + 2 * (size_t)h * h);
     }
     const int nl = (tile + 1) / 2;
     return (size_t)psize * (2 * 2 * (size_t)nl * (g.n + 1) + 2 * (size_t)g.n + g.n);
@@ -355,7 +382,7 @@ template <typename P>
 static cudaError_t launch_pass_t(const AxisGeom &g, const PassArgs &a, int ntiles, cudaStream_t st)
 {
     const size_t smem = scft_pass_smem_bytes(g, a.tile, a.h, (int)sizeof(P));
-    dim3 grid(ntiles, a.nchains);
+    const dim3 grid(ntiles, a.nchains);
     if (g.dirichlet)
         k_pass_dense<P><<<grid, 256, smem, st>>>(g, a);
     else
