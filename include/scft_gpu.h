@@ -229,7 +229,8 @@ int scft_batch_set_masks(scft_batch *b, int instance, const double *mask3);
 int scft_batch_set_iteration(scft_batch *b, int instance, unsigned long iter);
 int scft_batch_set_rng(scft_batch *b, int instance, const unsigned short seed[3]);
 int scft_batch_set_stop(scft_batch *b, int instance, double rms_tol);
-/* Stop an instance now (scft_freeze on its context); scft_batch_set_iteration re-arms it. */
+/* Stop an instance now (scft_freeze on its context); scft_batch_set_iteration re-arms it.
+ * scft_batch_run does not enqueue a group whose instances are all stopped. */
 int scft_batch_freeze(scft_batch *b, int instance);
 int scft_batch_get_fields(scft_batch *b, int instance, double *w14);
 int scft_batch_get_densities(scft_batch *b, int instance, double *phi13, double *phi_tot);

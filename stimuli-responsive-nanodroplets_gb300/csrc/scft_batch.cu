@@ -31,6 +31,8 @@ struct scft_batch {
     std::vector<int> group, slot;           /* [n] */
     std::vector<unsigned long> iter;        /* [n] current iIter */
     std::vector<scft_iter_out> last;        /* [n] latest record */
+    std::vector<char> idle;                 /* [n] frozen (converged or scft_batch_freeze) and not
+                                               re-armed since: a group of idle instances is not run */
 };
 
 /* Instances that can share a context: same grid, MASK, active fields and
@@ -66,6 +68,7 @@ extern "C" int scft_batch_create(const scft_surface *surfaces, int n, const scft
     b->slot.assign(n, -1);
     b->iter.assign(n, 0);
     b->last.assign(n, scft_iter_out{});
+    b->idle.assign(n, 0);
     std::map<std::string, int> by_key;
     for (int i = 0; i < n; ++i) {
         scft_derived d;
@@ -149,7 +152,10 @@ extern "C" int scft_batch_set_iteration(scft_batch *b, int i, unsigned long it)
 {
     LOCATE(b, i);
     int rc = scft_set_iteration(c_, s_, it);
-    if (rc == SCFT_OK) b->iter[i] = it;
+    if (rc == SCFT_OK) {
+        b->iter[i] = it;
+        b->idle[i] = 0; /* re-armed */
+    }
     return rc;
 }
 
@@ -168,7 +174,9 @@ extern "C" int scft_batch_set_stop(scft_batch *b, int i, double rms_tol)
 extern "C" int scft_batch_freeze(scft_batch *b, int i)
 {
     LOCATE(b, i);
-    return scft_freeze(c_, s_);
+    int rc = scft_freeze(c_, s_);
+    if (rc == SCFT_OK) b->idle[i] = 1;
+    return rc;
 }
 
 extern "C" int scft_batch_get_fields(scft_batch *b, int i, double *w14)
@@ -193,6 +201,12 @@ extern "C" int scft_batch_run(scft_batch *b, int max_iter, int chunk, scft_batch
     const int G = (int)b->ctx.size();
     std::vector<unsigned long> start(b->iter);
     std::vector<int> ran(G, 0), live(G, 1);
+    /* a group whose instances are all frozen would only repeat their records */
+    for (int g = 0; g < G; ++g) {
+        int all_idle = 1;
+        for (int i : b->members[g]) all_idle &= b->idle[i] ? 1 : 0;
+        if (all_idle) live[g] = 0;
+    }
     std::vector<std::vector<scft_iter_out>> recs(G);
     for (int g = 0; g < G; ++g) recs[g].resize((size_t)chunk * b->members[g].size());
     int status = SCFT_OK;
@@ -228,6 +242,7 @@ extern "C" int scft_batch_run(scft_batch *b, int max_iter, int chunk, scft_batch
                 const int i = b->members[g][s];
                 b->last[i] = r;
                 b->iter[i] = r.iter;
+                b->idle[i] = r.converged ? 1 : 0;
                 if (!r.converged) all_done = 0;
             }
             if (all_done || status != SCFT_OK) live[g] = 0;

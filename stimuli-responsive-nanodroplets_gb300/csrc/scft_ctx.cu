@@ -275,41 +275,6 @@ static int upload_p(scft_ctx *c, void **dst, const std::vector<double> &v)
     return upload(c, dst, f);
 }
 
-/* FP32x2 form: the column range of each row of a dense operator (row-major
- * n x n blocks A and, if given, B, ranges taken over both) outside of which
- * every entry is below 2^-60 of the largest entry. The heat kernel of one
- * contour step falls off like a Gaussian a grid spacing or so wide, so the
- * double-float z pass (rounding 2^-48) only sums the band; the other forms
- * keep the full product. */
-static int upload_band(scft_ctx *c, InstOps &o, int ai, const std::vector<double> &A, const std::vector<double> *B,
-                       int n)
-{
-    if (c->opt.precision != SCFT_PREC_FP32X2) return SCFT_OK;
-    double big = 0.0;
-    for (double v : A) big = fmax(big, fabs(v));
-    if (B)
-        for (double v : *B) big = fmax(big, fabs(v));
-    const double thr = ldexp(big, -60);
-    std::vector<int2> band(n);
-    for (int i = 0; i < n; ++i) {
-        int lo = n, hi = 0;
-        for (int j = 0; j < n; ++j) {
-            const double v = fmax(fabs(A[(size_t)i * n + j]), B ? fabs((*B)[(size_t)i * n + j]) : 0.0);
-            if (v > thr) {
-                lo = lo < j ? lo : j;
-                hi = j + 1;
-            }
-        }
-        if (lo >= hi) lo = hi = 0;
-        band[i] = make_int2(lo, hi);
-    }
-    void *d = nullptr;
-    int rc = upload(c, &d, band);
-    if (rc) return rc;
-    o.band[ai] = static_cast<const int2 *>(d);
-    return SCFT_OK;
-}
-
 /* Round an n x n operator block (row-major) to FP32 so that every column sum of
  * the FP32 values equals the FP64 column sum as closely as FP32 allows: each
  * entry is first rounded to nearest, then the residual of its column is handed
@@ -671,20 +636,15 @@ static int axis_tables(scft_ctx *c, const Axis &A, double alpha, InstOps &o, int
         void *ka = nullptr, *kb = nullptr;
         int rc = upload_p(c, &ka, At);
         if (!rc) rc = upload_p(c, &kb, Bt);
-        if (!rc) rc = upload_band(c, o, ai, Ar, &Br, h);
         if (rc) return rc;
         o.kA[ai] = ka;
         o.kB[ai] = kb;
     } else {
-        std::vector<double> Kt((size_t)n * n), Kr((size_t)n * n);
+        std::vector<double> Kt((size_t)n * n);
         for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) {
-                Kt[(size_t)j * n + i] = (double)K[(size_t)i * n + j];
-                Kr[(size_t)i * n + j] = (double)K[(size_t)i * n + j];
-            }
+            for (int j = 0; j < n; ++j) Kt[(size_t)j * n + i] = (double)K[(size_t)i * n + j];
         void *ka = nullptr;
         int rc = upload_p(c, &ka, Kt);
-        if (!rc) rc = upload_band(c, o, ai, Kr, nullptr, n);
         if (rc) return rc;
         o.kA[ai] = ka;
         o.kB[ai] = ka;

@@ -33,10 +33,6 @@
 struct InstOps {
     const void *kz, *twx, *ex;
     const void *spec[3], *tw[3], *kA[3], *kB[3];
-    /* FP32x2 form, dense axes: per output row i the columns [lo, hi) outside of
-     * which every operator entry is below 2^-60 of the largest (int2 per row);
-     * NULL elsewhere */
-    const int2 *band[3];
 };
 
 /* One propagator chain of one instance: q[0] from init, then len-1 contour

@@ -96,8 +96,10 @@ __device__ __forceinline__ int div_mag(int x, unsigned mag) { return mag ? (int)
 
 /* One Stockham autosort stage (Govindaraju et al., SC'08 formulation) over nl
  * complex lines of length n with line pitch ldl. tw[t] = exp(-2 pi i t / n).
- * r * k * tws < n for every butterfly input, so the twiddle index needs no
- * reduction modulo n. */
+ * The double-float stages divide by multiply-high with the host-computed
+ * reciprocals and index the twiddles without a reduction modulo n
+ * (r * k * tws < n); the FP32 and FP64 stages keep integer division, as
+ * measured fastest for them. */
 template <typename P, bool INV, int R>
 __device__ __forceinline__ void stockham_stage(const Cx<P> *__restrict__ a, Cx<P> *__restrict__ b, int n, int ldl,
                                                int nl, int Ns, unsigned mag_nr, unsigned mag_ns,
@@ -105,19 +107,20 @@ __device__ __forceinline__ void stockham_stage(const Cx<P> *__restrict__ a, Cx<P
 {
     const int nr = n / R;
     const int tws = n / (Ns * R);
+    constexpr bool DF = std::is_same<P, dfloat>::value;
     for (int w = threadIdx.x; w < nl * nr; w += blockDim.x) {
-        const int line = div_mag(w, mag_nr);
+        const int line = DF ? div_mag(w, mag_nr) : w / nr;
         const int j = w - line * nr;
         const Cx<P> *in = a + line * ldl;
         Cx<P> *out = b + line * ldl;
-        const int jq = div_mag(j, mag_ns);
+        const int jq = DF ? div_mag(j, mag_ns) : j / Ns;
         const int k = j - jq * Ns;
         Cx<P> v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             v[r] = in[j + r * nr];
             if (r > 0 && k > 0) {
-                Cx<P> t = tw[r * k * tws];
+                Cx<P> t = tw[DF ? r * k * tws : (r * k * tws) % n];
                 if (INV) t.y = -t.y;
                 v[r] = cmul(v[r], t);
             }
@@ -271,9 +274,10 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
     if (a.s >= cd.len - 1) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, h = a.h;
-    /* u and v rows have an odd pitch (h + 1 values): the two lines a warp can
-     * span then broadcast from different banks */
-    const int hp = h + 1;
+    /* double-float: u and v rows have an odd pitch (h + 1 values), so the two
+     * lines a warp can span broadcast from different banks (the space is
+     * reserved for every type; FP32 and FP64 keep the dense pitch h) */
+    const int hp = std::is_same<P, dfloat>::value ? h + 1 : h;
     P *x = reinterpret_cast<P *>(smem_raw);   /* tile * n */
     P *u = x + a.tile * n;                    /* tile * hp */
     P *v = u + a.tile * hp;                   /* tile * hp */
@@ -286,8 +290,6 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
     const P *bz = reinterpret_cast<const P *>(a.s < cd.seg_end ? cd.b0 : cd.b1);
     const P *gA = reinterpret_cast<const P *>(cd.ops->kA[a.axis]);
     const P *gB = reinterpret_cast<const P *>(cd.ops->kB[a.axis]);
-    /* the band of nonnegligible columns per row (FP32x2 form only) */
-    const int2 *band = std::is_same<P, dfloat>::value ? cd.ops->band[a.axis] : nullptr;
     for (int e = threadIdx.x; e < h * h; e += blockDim.x) {
         kA[e] = gA[e];
         if (a.even) kB[e] = gB[e];
@@ -325,13 +327,7 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
             DotOf<P> sacc, dacc;
             sacc.zero();
             dacc.zero();
-            int j0 = 0, j1 = h;
-            if (band) {
-                const int2 r = band[i];
-                j0 = r.x;
-                j1 = r.y;
-            }
-            for (int j = j0; j < j1; ++j) {
+            for (int j = 0; j < h; ++j) {
                 sacc.add(kA[j * h + i], ul[j]);
                 dacc.add(kB[j * h + i], vl[j]);
             }
@@ -352,13 +348,7 @@ __global__ void __launch_bounds__(256) k_pass_dense(AxisGeom g, PassArgs a)
             const P *xl = x + l * n;
             DotOf<P> dot;
             dot.zero();
-            int j0 = 0, j1 = n;
-            if (band) {
-                const int2 r = band[i];
-                j0 = r.x;
-                j1 = r.y;
-            }
-            for (int j = j0; j < j1; ++j) dot.add(kA[j * n + i], xl[j]);
+            for (int j = 0; j < n; ++j) dot.add(kA[j * n + i], xl[j]);
             P acc = dot.value();
             const long o0 = elem_offset<P>(g, L0 + l, i);
             if (a.last) acc *= bz[o0];

@@ -108,11 +108,6 @@ class FinishedResult:
     status: int
 
 
-def _freeze(b: Batch, i: int):
-    """An instance stops at the end of its next iteration (any RMS is below the tolerance)."""
-    b.set_stop(i, 1e300)
-
-
 def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: int, switch_rms: float = SWITCH_RMS,
                  chunk: int = 200, use_graph: bool = True, stall_round: int = STALL_ROUND,
                  stall_gain: float = STALL_GAIN, floor_rms: float = FLOOR_RMS, finish: str = "fp32x2"):
@@ -138,6 +133,7 @@ def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: 
     out: List[Optional[FinishedResult]] = [None] * n
     handq: "queue.Queue" = queue.Queue()
     errors: list = []
+    abort = threading.Event()            # the FP32 loop failed: the finisher stops at its next round
     b = make_batch(surfaces, inputs, "fp32", rms_tol, use_graph)
     bf = None
     try:
@@ -152,7 +148,7 @@ def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: 
             ran = {}                     # instance -> iterations in the finishing form
             fp32_over = False
             try:
-                while True:
+                while not abort.is_set():
                     pending = []
                     if not live and not fp32_over:
                         pending.append(handq.get())          # idle: wait for the next hand-over
@@ -205,16 +201,19 @@ def run_finished(surfaces: Sequence[Surface], inputs, rms_tol: float, max_iter: 
                     done = r.converged or r.status != 0 or used[i] >= max_iter
                     if not done and r.rms < switch_rms and (r.rms > stall_gain * last_rms[i] or r.rms < floor_rms):
                         handq.put((i, b.get_fields(i), r.iter, used[i]))
-                        _freeze(b, i)
+                        b.freeze(i)
                         active.discard(i)
                     elif done:
                         out[i] = FinishedResult(used[i], used[i], r.rms, r.free_energy, bool(r.converged), r.status)
-                        _freeze(b, i)
+                        b.freeze(i)
                         active.discard(i)
                     last_rms[i] = r.rms
                 if errors:
                     break
             t1 = time.perf_counter()
+        except BaseException:
+            abort.set()
+            raise
         finally:
             handq.put(None)
             th.join()
