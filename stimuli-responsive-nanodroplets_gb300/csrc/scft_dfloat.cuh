@@ -18,11 +18,13 @@
  * |x| + |y| (not of |x + y|): the same normwise bound an FFT or a dot product
  * has in any precision. Every operation goes through the _rn intrinsics,
  * which the compiler never contracts into an FMA: a contraction would break
- * the error-free transforms.
+ * the error-free transforms. The same code compiles for the host, where the
+ * tests check it against long double.
  */
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 
 struct dfloat {
     float hi, lo;
@@ -37,78 +39,127 @@ struct dfloat {
 
 namespace dfo {
 
-/* s + e == a + b exactly (Knuth) */
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+/* The FP32 primitives, each rounded to nearest and never contracted: the _rn
+ * intrinsics on the device; on the host (unit tests of these algorithms)
+ * IEEE float operations whose results pass through a volatile, so no
+ * multiply is fused into a following add, and the C99 fused multiply-add. */
+__host__ __device__ __forceinline__ float f_add(float a, float b)
 {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    volatile float r = a + b;
+    return r;
+#endif
+}
+__host__ __device__ __forceinline__ float f_sub(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    volatile float r = a - b;
+    return r;
+#endif
+}
+__host__ __device__ __forceinline__ float f_mul(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    volatile float r = a * b;
+    return r;
+#endif
+}
+__host__ __device__ __forceinline__ float f_fma(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+__host__ __device__ __forceinline__ float f_div(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(a, b);
+#else
+    volatile float r = a / b;
+    return r;
+#endif
+}
+
+/* s + e == a + b exactly (Knuth) */
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = f_add(a, b);
+    const float bb = f_sub(s, a);
+    e = f_add(f_sub(a, f_sub(s, bb)), f_sub(b, bb));
 }
 
 /* s + e == a + b exactly when |a| >= |b| or a == 0 (Dekker) */
-__device__ __forceinline__ dfloat fast_two_sum(float a, float b)
+__host__ __device__ __forceinline__ dfloat fast_two_sum(float a, float b)
 {
-    const float s = __fadd_rn(a, b);
-    return dfloat(s, __fsub_rn(b, __fsub_rn(s, a)));
+    const float s = f_add(a, b);
+    return dfloat(s, f_sub(b, f_sub(s, a)));
 }
 
-__device__ __forceinline__ dfloat add(dfloat x, dfloat y)
+__host__ __device__ __forceinline__ dfloat add(dfloat x, dfloat y)
 {
     float s, e;
     two_sum(x.hi, y.hi, s, e);
-    e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    e = f_add(e, f_add(x.lo, y.lo));
     return fast_two_sum(s, e);
 }
 
-__device__ __forceinline__ dfloat neg(dfloat x) { return dfloat(-x.hi, -x.lo); }
+__host__ __device__ __forceinline__ dfloat neg(dfloat x) { return dfloat(-x.hi, -x.lo); }
 
-__device__ __forceinline__ dfloat mul(dfloat x, dfloat y)
+__host__ __device__ __forceinline__ dfloat mul(dfloat x, dfloat y)
 {
-    const float p = __fmul_rn(x.hi, y.hi);
-    float e = __fmaf_rn(x.hi, y.hi, -p);
-    e = __fadd_rn(e, __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.hi)));
+    const float p = f_mul(x.hi, y.hi);
+    float e = f_fma(x.hi, y.hi, -p);
+    e = f_add(e, f_fma(x.hi, y.lo, f_mul(x.lo, y.hi)));
     return fast_two_sum(p, e);
 }
 
 /* x*y - u*v with one renormalisation (the real or imaginary part of a complex product) */
-__device__ __forceinline__ dfloat mul_sub(dfloat x, dfloat y, dfloat u, dfloat v)
+__host__ __device__ __forceinline__ dfloat mul_sub(dfloat x, dfloat y, dfloat u, dfloat v)
 {
-    const float p = __fmul_rn(x.hi, y.hi);
-    const float q = __fmul_rn(u.hi, v.hi);
-    const float ep = __fmaf_rn(x.hi, y.hi, -p);
-    const float eq = __fmaf_rn(u.hi, v.hi, -q);
+    const float p = f_mul(x.hi, y.hi);
+    const float q = f_mul(u.hi, v.hi);
+    const float ep = f_fma(x.hi, y.hi, -p);
+    const float eq = f_fma(u.hi, v.hi, -q);
     float s, e;
     two_sum(p, -q, s, e);
-    float t = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.hi));
-    t = __fsub_rn(t, __fmaf_rn(u.hi, v.lo, __fmul_rn(u.lo, v.hi)));
-    e = __fadd_rn(e, __fadd_rn(__fsub_rn(ep, eq), t));
+    float t = f_fma(x.hi, y.lo, f_mul(x.lo, y.hi));
+    t = f_sub(t, f_fma(u.hi, v.lo, f_mul(u.lo, v.hi)));
+    e = f_add(e, f_add(f_sub(ep, eq), t));
     return fast_two_sum(s, e);
 }
 
 /* x*y + u*v */
-__device__ __forceinline__ dfloat mul_add(dfloat x, dfloat y, dfloat u, dfloat v)
+__host__ __device__ __forceinline__ dfloat mul_add(dfloat x, dfloat y, dfloat u, dfloat v)
 {
     return mul_sub(x, y, neg(u), v);
 }
 
 /* Division: one FP32 quotient, the remainder x - q*y in double-float, one
  * correction term (the double-word division of the paper above). */
-__device__ __forceinline__ dfloat div(dfloat x, dfloat y)
+__host__ __device__ __forceinline__ dfloat div(dfloat x, dfloat y)
 {
-    const float q = __fdiv_rn(x.hi, y.hi);
+    const float q = f_div(x.hi, y.hi);
     const dfloat r = add(x, neg(mul(dfloat(q, 0.0f), y)));
-    return fast_two_sum(q, __fdiv_rn(r.hi, y.hi));
+    return fast_two_sum(q, f_div(r.hi, y.hi));
 }
 
 } // namespace dfo
 
-__device__ __forceinline__ dfloat operator+(dfloat x, dfloat y) { return dfo::add(x, y); }
-__device__ __forceinline__ dfloat operator-(dfloat x, dfloat y) { return dfo::add(x, dfo::neg(y)); }
-__device__ __forceinline__ dfloat operator-(dfloat x) { return dfo::neg(x); }
-__device__ __forceinline__ dfloat operator*(dfloat x, dfloat y) { return dfo::mul(x, y); }
-__device__ __forceinline__ dfloat operator/(dfloat x, dfloat y) { return dfo::div(x, y); }
-__device__ __forceinline__ dfloat &operator+=(dfloat &x, dfloat y) { return x = x + y; }
-__device__ __forceinline__ dfloat &operator*=(dfloat &x, dfloat y) { return x = x * y; }
+__host__ __device__ __forceinline__ dfloat operator+(dfloat x, dfloat y) { return dfo::add(x, y); }
+__host__ __device__ __forceinline__ dfloat operator-(dfloat x, dfloat y) { return dfo::add(x, dfo::neg(y)); }
+__host__ __device__ __forceinline__ dfloat operator-(dfloat x) { return dfo::neg(x); }
+__host__ __device__ __forceinline__ dfloat operator*(dfloat x, dfloat y) { return dfo::mul(x, y); }
+__host__ __device__ __forceinline__ dfloat operator/(dfloat x, dfloat y) { return dfo::div(x, y); }
+__host__ __device__ __forceinline__ dfloat &operator+=(dfloat &x, dfloat y) { return x = x + y; }
+__host__ __device__ __forceinline__ dfloat &operator*=(dfloat &x, dfloat y) { return x = x * y; }
 
 /* Dot-product accumulator: the running sum's high part is kept error-free
  * (TwoSum), product errors (TwoProd) and cross terms go to an FP32 low part,
@@ -116,17 +167,17 @@ __device__ __forceinline__ dfloat &operator*=(dfloat &x, dfloat y) { return x = 
  * and Oishi, extended to double-float operands). 12 FP32 instructions a term. */
 struct DotDF {
     float hi, lo;
-    __device__ __forceinline__ void zero() { hi = lo = 0.0f; }
-    __device__ __forceinline__ void add(dfloat a, dfloat b)
+    __host__ __device__ __forceinline__ void zero() { hi = lo = 0.0f; }
+    __host__ __device__ __forceinline__ void add(dfloat a, dfloat b)
     {
-        const float p = __fmul_rn(a.hi, b.hi);
-        float e = __fmaf_rn(a.hi, b.hi, -p);
-        e = __fmaf_rn(a.hi, b.lo, e);
-        e = __fmaf_rn(a.lo, b.hi, e);
+        const float p = dfo::f_mul(a.hi, b.hi);
+        float e = dfo::f_fma(a.hi, b.hi, -p);
+        e = dfo::f_fma(a.hi, b.lo, e);
+        e = dfo::f_fma(a.lo, b.hi, e);
         float s, se;
         dfo::two_sum(hi, p, s, se);
         hi = s;
-        lo = __fadd_rn(lo, __fadd_rn(se, e));
+        lo = dfo::f_add(lo, dfo::f_add(se, e));
     }
-    __device__ __forceinline__ dfloat value() const { return dfo::fast_two_sum(hi, lo); }
+    __host__ __device__ __forceinline__ dfloat value() const { return dfo::fast_two_sum(hi, lo); }
 };
