@@ -33,6 +33,7 @@ struct dfloat {
     __host__ __device__ constexpr dfloat(float h, float l) : hi(h), lo(l) {}
     /* nearest pair to a double: hi = fl32(d), lo = fl32(d - hi) (d - hi is exact in FP64) */
     __host__ __device__ constexpr dfloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+    /* an int exactly (through the exact double; at run time a few FP64 conversions) */
     __host__ __device__ constexpr dfloat(int i) : dfloat((double)i) {}
     __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };

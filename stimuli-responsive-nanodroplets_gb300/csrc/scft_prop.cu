@@ -22,7 +22,8 @@
  * The kernels are written once over the value type P: double (plain form),
  * float (per-axis passes of the FP32 form) and dfloat (the FP32x2 form: slices,
  * Boltzmann factors and operator tables stored as FP32 pairs, every operation
- * in double-float arithmetic, no FP64 instruction on the contour path).
+ * in double-float arithmetic; FP64 only converts the line length for the mean
+ * mode's division).
  */
 #include <cuda_runtime.h>
 

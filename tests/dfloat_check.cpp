@@ -70,6 +70,14 @@ int main()
         wdot.see(val(d.value()) - exact, 48 * 2 * U * mag);
     }
     int bad = 0;
+    /* integers convert exactly (the FFT pass divides the mean mode by the line length) */
+    for (long long i : {0LL, 1LL, -1LL, 192LL, 16777217LL, -16777219LL, 2147483647LL, -2147483647LL - 1}) {
+        const dfloat d((int)i);
+        if (val(d) != (LD)i) {
+            printf("int %lld converts to %.21Lg\n", i, val(d));
+            bad = 1;
+        }
+    }
     for (const Worst *w : {&wadd, &wmul, &wms, &wdiv, &wdot, &wnorm}) {
         printf("%-10s worst error / bound = %.3f\n", w->name, w->ratio);
         if (!(w->ratio <= 1.0)) bad = 1;
